@@ -1,0 +1,203 @@
+/*
+ * gxgpu.h — C ABI of libgxgpu.so, the GB300 (sm_103a) graph-build step of Genomix.
+ *
+ * The graph-build step reads sequencing reads, extracts every k-mer, canonicalises it
+ * against its reverse complement and aggregates the occurrences into de Bruijn Node
+ * records.  The records are byte-compatible with genomix-data's Writables, so a
+ * SequenceFile<VKmer, Node> written from them is read unchanged by the genomix-pregelix
+ * cleaning jobs (genomix-pregelix/.../base/BinaryVertexInputFormat.java:25).
+ *
+ * Reference interfaces this ABI replaces (paths inside the genomix project):
+ *   - GenomixHyracksDriver.runJob(conf, Plan.BUILD_DEBRUIJN_GRAPH, profile)
+ *       genomix-hyracks/.../graph/driver/GenomixHyracksDriver.java:84-135
+ *   - the three operator plug-ins wired by JobGenBuildBrujinGraph.assignJob (:79-154):
+ *       IKeyValueParserFactory  ReadsKeyValueParserFactory.java:95-254
+ *       IAggregatorDescriptorFactory  AggregateKmerAggregateFactory.java:93-214
+ *       ITupleWriterFactory  KmerNodePairSequenceWriterFactory.java:66-94
+ *   - the FASTQ -> readid conversion GenomixDriver.convertAndUploadFastqToHDFS
+ *       genomix-driver/.../driver/GenomixDriver.java:665-714
+ *
+ * Conventions
+ *   - Every call returns a gx_status; no C++ exception crosses the ABI.
+ *   - Host buffers passed in are borrowed for the duration of the call only.
+ *   - Device buffers passed in (the *_device calls) are borrowed until gx_job_run returns.
+ *   - The library owns all device tables; they live until gx_job_destroy.
+ *   - k is a per-job value: there is no process-wide k (the reference keeps it in a
+ *     JVM-wide static, Kmer.java:41-54).
+ *   - A gx_ctx owns one CUDA stream.  Distinct gx_job objects may be driven from
+ *     different host threads; submissions on one context are serialised by a lock.
+ */
+#ifndef GXGPU_H
+#define GXGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The parse errors reproduce the exceptions that abort the reference job. */
+typedef enum gx_status {
+    GX_OK = 0,
+    GX_EINVAL = 1,            /* bad argument: null pointer, k outside 3..64, bad option */
+    GX_EINVAL_LINE = 2,       /* a readid line does not split into 2 or 3 tab fields:
+                                 IllegalStateException, ReadsKeyValueParserFactory.java:118-122 */
+    GX_EINVAL_NUMBER = 3,     /* readId field is not a Java long: NumberFormatException from
+                                 Long.parseLong, ReadsKeyValueParserFactory.java:112,115 */
+    GX_EREADID_RANGE = 4,     /* readId outside [0, 2^35): IllegalArgumentException,
+                                 ReadHeadInfo.makeUUID, ReadHeadInfo.java:110-113 */
+    GX_EREAD_TOO_SHORT = 5,   /* k >= read length: IllegalArgumentException,
+                                 ReadsKeyValueParserFactory.java:152-155 */
+    GX_ENOMEM = 6,            /* device or pinned allocation failed */
+    GX_ETABLE_FULL = 7,       /* a hash-table partition overflowed its probe limit */
+    GX_ETIMEOUT = 8,          /* a bounded device wait ran out */
+    GX_ECUDA = 9,             /* a CUDA runtime call failed */
+    GX_ESTATE = 10,           /* call out of order (e.g. emit before run) */
+    GX_ECANCELLED = 11,       /* job cancelled (serving) */
+    GX_EFASTQ_PAIRING = 12,   /* paired FASTQ streams differ in line count: IOException,
+                                 GenomixDriver.java:682-686 */
+    GX_EBUSY = 13,            /* serving: no admission slot or memory right now */
+    GX_EAGAIN = 14            /* serving: result not ready yet */
+} gx_status;
+
+/* Text of a status code (static storage). */
+const char *gx_status_str(gx_status s);
+
+/* Input kinds (gx_job_opts.input_kind). */
+enum {
+    GX_INPUT_READID = 0,      /* "readId \t seq [\t mateSeq]" lines, as the graph build reads */
+    GX_INPUT_FASTQ = 1        /* FASTQ; converted with the reference's readId = 4*i+2 rule */
+};
+
+typedef struct gx_ctx gx_ctx;
+typedef struct gx_job gx_job;
+
+typedef struct gx_ctx_opts {
+    size_t struct_size;       /* sizeof(gx_ctx_opts) */
+    size_t device_mem_limit;  /* bytes the context may hold on the device; 0 = 90% of free */
+    int flags;                /* reserved, 0 */
+} gx_ctx_opts;
+
+typedef struct gx_job_opts {
+    size_t struct_size;       /* sizeof(gx_job_opts) */
+    int kmer_length;          /* GenomixJobConf.KMER_LENGTH; 3..64 (64-bit keys k<=32, 128-bit k<=64) */
+    int input_kind;           /* GX_INPUT_READID or GX_INPUT_FASTQ */
+    int paired;               /* FASTQ only: 1 = mate streams 0 and 1 are paired files */
+    int out_parts;            /* output parts (SequenceFile part files); 0 means 1 */
+    double load_factor;       /* table slots = occurrences / load_factor; 0 = default (0.5) */
+    int max_readids_per_edge; /* accepted and ignored, as in the reference (GenomixJobConf.java:718) */
+    int threads_per_read;     /* 0 = autotuned; 1 = thread per read; 32 = warp per read */
+    size_t est_input_bytes;   /* capacity hint for the device input buffer; 0 = grow on demand */
+} gx_job_opts;
+
+typedef struct gx_stats {
+    uint64_t lines;           /* input lines (readid) or records (FASTQ) */
+    uint64_t reads;           /* mates that passed the [ACGTacgt]+ filter */
+    uint64_t kmers;           /* k-mer occurrences: sum over valid mates of (L - k + 1) */
+    uint64_t nodes;           /* distinct canonical k-mers = output records */
+    uint64_t read_heads;      /* read heads attached to nodes */
+    uint64_t record_bytes;    /* bytes of the serialized record stream */
+    uint64_t table_slots;     /* hash-table slots allocated */
+    uint64_t table_partitions;
+    uint64_t error_line;      /* 1-based line (or FASTQ record) that failed; 0 if none */
+    uint64_t cov_inexact_nodes; /* nodes with count >= 2^24 (float coverage no longer exact) */
+    uint32_t max_probe;       /* longest probe sequence seen during inserts */
+    uint32_t key_bits;        /* 64 or 128 */
+    double ms_parse;          /* device time of the parse kernels */
+    double ms_insert;         /* device time of k-mer extraction + table inserts */
+    double ms_emit;           /* device time of compaction + record serialization */
+    double ms_total;          /* device time of gx_job_run */
+} gx_stats;
+
+/* ---- context ------------------------------------------------------------------------- */
+
+/* Create a context on CUDA device `device`.  opts may be NULL.  Replaces the connection to
+ * the Hyracks cluster controller made in GenomixHyracksDriver.java:70-78. */
+gx_status gx_ctx_create(int device, const gx_ctx_opts *opts, gx_ctx **out);
+void gx_ctx_destroy(gx_ctx *ctx);
+
+/* ---- plain (one job per launch sequence) ---------------------------------------------- */
+
+/* Create a graph-build job.  Replaces JobGenBuildBrujinGraph's construction from a
+ * GenomixJobConf (JobGenBuildBrujinGraph.java:79-90, JobGen.java:61-111). */
+gx_status gx_job_create(gx_ctx *ctx, const gx_job_opts *opts, gx_job **out);
+
+/* Append input bytes from host memory (any host memory; pinned is fastest).  Each call is
+ * one input file: a final line without a terminator is still a line, as Hadoop's
+ * LineRecordReader reads it.  For readid input mate_stream must be 0; for paired FASTQ,
+ * 0 and 1 are the two mate files.  Replaces the HDFS read of the input splits
+ * (HDFSReadOperatorDescriptor.java:98-143). */
+gx_status gx_job_add_input(gx_job *job, const void *host, size_t bytes, int mate_stream);
+
+/* Same, from device memory.  The pointer must be 16-byte aligned and stay valid until
+ * gx_job_run returns.  No copy is made for a single readid input. */
+gx_status gx_job_add_input_device(gx_job *job, const void *dev, size_t bytes, int mate_stream);
+
+/* Build the graph on the device: parse, k-mer extraction, canonicalisation, aggregation
+ * and serialization of every (VKmer, Node) record.  Replaces the parse -> sort -> group ->
+ * merge -> group pipeline of JobGenBuildBrujinGraph.generateGroupbyKmerJob (:92-117).
+ * Returns the first parse error by line order, with gx_stats.error_line set. */
+gx_status gx_job_run(gx_job *job);
+
+/* Copy the serialized records of output part `part` to host memory.  The stream is a
+ * concatenation of SequenceFile record bodies: int32 BE record length, int32 BE key length,
+ * VKmer key, Node value (the bytes SequenceFile.Writer.append writes for one record,
+ * KmerNodePairSequenceWriterFactory.java:79-94).  Repeated calls continue where the last
+ * stopped; *more is 1 while bytes remain.  Each call ends on a record boundary. */
+gx_status gx_job_emit(gx_job *job, int part, void *host_out, size_t cap, size_t *written, int *more);
+
+/* Device view of the whole record stream (all parts in order) and the per-part byte
+ * offsets (out_parts + 1 entries, host memory, owned by the job). */
+gx_status gx_job_records_device(gx_job *job, const void **dev, size_t *bytes,
+                                const uint64_t **part_offsets);
+
+/* Statistics of the last gx_job_run. */
+gx_status gx_job_stats(const gx_job *job, gx_stats *out);
+
+void gx_job_destroy(gx_job *job);
+
+/* ---- batched: many jobs in one persistent launch ------------------------------------- */
+
+/* Run n jobs of one context together.  Every job must have its inputs added and not yet
+ * have run.  Each job gets its own table partition range, k and output; the result of
+ * every job is identical to its gx_job_run result.  Per-job status codes go to
+ * statuses[i] (may be NULL); the call returns the first non-OK status. */
+gx_status gx_batch_run(gx_ctx *ctx, gx_job **jobs, int n, gx_status *statuses);
+
+/* ---- host helpers -------------------------------------------------------------------- */
+
+/* Page-locked host memory, suitable for direct ByteBuffers / FFM MemorySegments. */
+gx_status gx_pinned_alloc(size_t bytes, void **out);
+void gx_pinned_free(void *ptr);
+
+/* Convert FASTQ to readid text exactly as GenomixDriver.convertAndUploadFastqToHDFS does
+ * (GenomixDriver.java:665-714): record i gets readId 4*i+2; sequence lines are trimmed;
+ * paired input writes "id \t mate1 \t mate2".  mate2 may be NULL for single-end input.
+ * *out is allocated with malloc; free it with gx_host_free. */
+gx_status gx_fastq_to_readid(const void *mate1, size_t bytes1, const void *mate2, size_t bytes2,
+                             char **out, size_t *out_bytes);
+void gx_host_free(void *ptr);
+
+/* Write one Hadoop SequenceFile (version 6, uncompressed, key class
+ * edu.uci.ics.genomix.data.types.VKmer, value class edu.uci.ics.genomix.data.types.Node)
+ * from a record stream as returned by gx_job_emit.  sync (16 bytes) is the file's sync
+ * marker; NULL derives a deterministic marker from `seed`.  Replaces the SequenceFile.Writer
+ * opened in KmerNodePairSequenceWriterFactory.java:66-73.  *out is malloc'ed. */
+gx_status gx_seqfile_write(const void *records, size_t bytes, const uint8_t *sync, uint64_t seed,
+                           uint8_t **out, size_t *out_bytes);
+
+/* Extract the record stream from a SequenceFile written by gx_seqfile_write or by Hadoop
+ * (uncompressed).  *out is malloc'ed. */
+gx_status gx_seqfile_read(const void *file, size_t bytes, uint8_t **out, size_t *out_bytes);
+
+/* Text dump of a record stream, one line per record in the form
+ * key.toString() + "\t" + value.toString() that GenomixClusterManager.copyBinAndTextToLocal
+ * writes (GenomixClusterManager.java:371; Node.toString Node.java:524-537).  *out is malloc'ed. */
+gx_status gx_records_to_text(const void *records, size_t bytes, char **out, size_t *out_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GXGPU_H */
