@@ -1,0 +1,313 @@
+"""bench.py — k-mers/s of the GB300 graph build on the 5 Mbp paired-end workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step = one complete graph build (parse, k-mer extraction, canonicalisation,
+aggregation, serialization of every (VKmer, Node) record) of the workload:
+5 Mbp genome at GC 50% with 10 x 1 kbp segments repeated 10 times, 833,333 pairs of
+2 x 150 bp (50x), insert N(500, 50), 1% substitutions, 0.01% N, k = 31 (seeded synthetic
+reads, see genomix_gb300/synth.py).
+
+  value      k-mers/s with the readid text already in HBM (CUDA events on the library's
+             stream over K steps; the text (258 MB) and the table (6.3 GB) exceed L2, so no
+             flush is needed between steps)
+  e2e        the same metric through the C ABI with host buffers: pinned readid text in,
+             H2D copy, build, D2H copy of every record into pinned memory, per step
+  roofline   the table-insert kernel (k_insert): 64 B per k-mer occurrence (one 32 B sector
+             read + one written back) against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (C++ restatement of the reference's sort + group graph build) on
+             the first pairs of the same workload, all host threads
+
+With --impl reference the oracle itself is the measured implementation (the reference is
+Java 7 on Hyracks and cannot run on the box).  With N > 1 (torchrun) every rank builds its
+own replica of the workload (the build does not shard across GPUs; replicas only).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k-mers/s, bit-exact graph build, batched vs per-job, 1 GB300; p99 job latency"
+UNIT = "k-mers/s"
+CPU_SAMPLE_PAIRS = 120_000
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_insert_pe5mbp_ncu.txt")
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kmers):
+    """DRAM bytes per k_insert launch from the committed ncu summary, scaled to this launch's
+    occurrences (the capture runs a smaller case; traffic grows with the occurrences)."""
+    if not os.path.exists(PROFILE_TRAFFIC):
+        return None
+    per_occ = None
+    with open(PROFILE_TRAFFIC) as f:
+        for line in f:
+            if line.startswith("dram_bytes_per_occurrence:"):
+                per_occ = float(line.split(":")[1])
+    return None if per_occ is None else per_occ * kmers
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(text_sample, k, pairs, warm=False):
+    from oracle import gx_oracle as go
+    threads = os.cpu_count() or 1
+    if warm:
+        go.build_graph(text_sample[: len(text_sample) // 20], k, threads=threads, parts=threads)
+    t0 = time.perf_counter()
+    r = go.build_graph(text_sample, k, threads=threads, parts=threads)
+    dt = time.perf_counter() - t0
+    assert r.status == 0
+    return {"value": r.kmers / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {pairs} pairs of the workload ({r.kmers} k-mer occurrences), "
+                      f"oracle sort+group build, {threads} threads, {dt:.2f} s"}, r
+
+
+def workload(max_pairs=None):
+    from genomix_gb300 import synth
+    return synth.pe_5mbp(max_pairs=max_pairs)
+
+
+def config_of(w, n):
+    return {"workload": w.name, "genome_bp": w.genome_len, "pairs": w.reads, "read_len": 150, "k": w.k,
+            "input_bytes": len(w.text), "parallelism": f"replicas{n}" if n > 1 else "single",
+            "l2": "inputs and table larger than L2 (129 MB); no flush"}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    w = workload(args.max_pairs)
+    sample = sample_prefix(w.text, CPU_SAMPLE_PAIRS)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb, r = cpu_baseline(sample, w.k, CPU_SAMPLE_PAIRS)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r.kmers / v * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8/int64", "data": "synthetic (seeded)", "config": config_of(w, 1),
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def sample_prefix(text, pairs):
+    idx = -1
+    for _ in range(pairs):
+        idx = text.find(b"\n", idx + 1)
+        if idx < 0:
+            return text
+    return text[: idx + 1]
+
+
+def run_gb300(args, ws, rank, local):
+    import torch
+    import genomix_gb300 as gx
+
+    w = workload(args.max_pairs)
+    ctx = gx.Context(local)
+    torch.cuda.set_device(local)
+    d_text = torch.frombuffer(bytearray(w.text), dtype=torch.uint8).to(f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def step_device():
+        job = gx.GraphBuildJob(ctx, w.k)
+        job.add_input_device(d_text.data_ptr(), d_text.numel())
+        job.run()
+        st = job.stats()
+        job.close()
+        return st
+
+    for _ in range(args.warmup):
+        st0 = step_device()
+    barrier(ws)
+    torch.cuda.synchronize()
+    stats = []
+    with ClockSampler(local) as clk:
+        ctx.mark(0)
+        for _ in range(args.steps):
+            stats.append(step_device())
+        ctx.mark(1)
+        ms = ctx.elapsed_ms(0, 1)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms_max = max_over_ranks(ws, ms)
+    kmers = stats[0]["kmers"]
+    value = ws * args.steps * kmers / (ms_max / 1e3)
+
+    # ---- e2e: host buffers through the C ABI ----
+    pin_in = gx.PinnedBuffer(len(w.text))
+    pin_in.array()[:] = memoryview(w.text)
+    out_bytes = stats[0]["record_bytes"]
+    pin_out = gx.PinnedBuffer(out_bytes + 16)
+
+    def step_e2e():
+        job = gx.GraphBuildJob(ctx, w.k)
+        job.add_input(pin_in)
+        job.run()
+        wr, more = job.emit_into(0, pin_out.ptr, pin_out.nbytes)
+        assert not more and wr == out_bytes
+        job.close()
+
+    for _ in range(max(1, args.warmup // 2)):
+        step_e2e()
+    barrier(ws)
+    ctx.mark(2)
+    for _ in range(args.steps):
+        step_e2e()
+    ctx.mark(3)
+    ms_e2e = max_over_ranks(ws, ctx.elapsed_ms(2, 3))
+    e2e_value = ws * args.steps * kmers / (ms_e2e / 1e3)
+
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    ins_ms = statistics.mean(s["ms_insert"] for s in stats)
+    achieved = 64.0 * kmers / (ins_ms / 1e3) / 1e9
+    traffic = profiled_traffic(kmers)
+    b_alg = len(w.text) + 64.0 * kmers + out_bytes
+    job_ms = ms / args.steps
+    cb = None
+    if not args.no_cpu_baseline:
+        cb, _ = cpu_baseline(sample_prefix(w.text, CPU_SAMPLE_PAIRS), w.k, CPU_SAMPLE_PAIRS)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u8/int64", "data": "synthetic (seeded reads of the named shapes)",
+        "config": config_of(w, ws),
+        "reads_per_s": value / kmers * stats[0]["reads"],
+        "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": len(w.text),
+                "d2h_bytes_per_step": out_bytes, "ms_per_step": ms_e2e / args.steps},
+        "roofline": {"bound": "hbm", "kernel": "k_insert", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth",
+                     "traffic": traffic, "alg_bytes_per_unit": 64, "units_per_launch": kmers},
+        "job_roofline": {"alg_bytes": b_alg, "achieved_gbs": b_alg / (job_ms / 1e3) / 1e9,
+                         "frac": b_alg / (job_ms / 1e3) / 1e9 / peak},
+        "phases_ms": {"parse": statistics.mean(s["ms_parse"] for s in stats), "insert": ins_ms,
+                      "emit": statistics.mean(s["ms_emit"] for s in stats), "job": job_ms},
+        "graph": {"kmers": kmers, "reads": stats[0]["reads"], "nodes": stats[0]["nodes"],
+                  "read_heads": stats[0]["read_heads"], "record_bytes": out_bytes,
+                  "table_slots": stats[0]["table_slots"], "max_probe": stats[0]["max_probe"]},
+        "clocks": clk.summary(),
+        "cpu_baseline": cb,
+    }
+    print(json.dumps(line), flush=True)
+    pin_in.close()
+    pin_out.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--max-pairs", type=int, default=None,
+                    help="use only the first pairs of the workload (profiling captures)")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_gb300(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,109 @@
+"""ctypes binding of libgxgpu.so (include/gxgpu.h).
+
+The library is built in-tree by genomix_gb300.build; importing this module fails loudly
+when it is missing — there is no CPU fallback.
+"""
+import ctypes
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libgxgpu.so")
+
+GX_OK = 0
+STATUS_NAMES = {
+    0: "GX_OK", 1: "GX_EINVAL", 2: "GX_EINVAL_LINE", 3: "GX_EINVAL_NUMBER", 4: "GX_EREADID_RANGE",
+    5: "GX_EREAD_TOO_SHORT", 6: "GX_ENOMEM", 7: "GX_ETABLE_FULL", 8: "GX_ETIMEOUT", 9: "GX_ECUDA",
+    10: "GX_ESTATE", 11: "GX_ECANCELLED", 12: "GX_EFASTQ_PAIRING", 13: "GX_EBUSY", 14: "GX_EAGAIN",
+}
+INPUT_READID, INPUT_FASTQ = 0, 1
+
+# every symbol include/gxgpu.h declares
+EXPORTS = [
+    "gx_status_str", "gx_ctx_create", "gx_ctx_destroy", "gx_ctx_mark", "gx_ctx_elapsed_ms", "gx_ctx_synchronize",
+    "gx_job_create", "gx_job_add_input", "gx_job_add_input_device", "gx_job_run", "gx_job_emit",
+    "gx_job_records_device", "gx_job_stats", "gx_job_destroy", "gx_batch_run", "gx_pinned_alloc",
+    "gx_pinned_free", "gx_fastq_to_readid", "gx_host_free", "gx_seqfile_write", "gx_seqfile_read",
+    "gx_records_to_text",
+]
+
+
+class CtxOpts(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("device_mem_limit", ctypes.c_size_t), ("flags", ctypes.c_int)]
+
+
+class JobOpts(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_size_t),
+        ("kmer_length", ctypes.c_int),
+        ("input_kind", ctypes.c_int),
+        ("paired", ctypes.c_int),
+        ("out_parts", ctypes.c_int),
+        ("load_factor", ctypes.c_double),
+        ("max_readids_per_edge", ctypes.c_int),
+        ("threads_per_read", ctypes.c_int),
+        ("est_input_bytes", ctypes.c_size_t),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("lines", ctypes.c_uint64), ("reads", ctypes.c_uint64), ("kmers", ctypes.c_uint64),
+        ("nodes", ctypes.c_uint64), ("read_heads", ctypes.c_uint64), ("record_bytes", ctypes.c_uint64),
+        ("table_slots", ctypes.c_uint64), ("table_partitions", ctypes.c_uint64), ("error_line", ctypes.c_uint64),
+        ("cov_inexact_nodes", ctypes.c_uint64), ("max_probe", ctypes.c_uint32), ("key_bits", ctypes.c_uint32),
+        ("kernel_launches", ctypes.c_uint64),
+        ("ms_parse", ctypes.c_double), ("ms_insert", ctypes.c_double), ("ms_emit", ctypes.c_double),
+        ("ms_total", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def load():
+    """Loads libgxgpu.so; raises when it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m genomix_gb300.build` "
+                          "(the graph build has no CPU fallback)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, sz, i, P = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER
+    sig = {
+        "gx_status_str": ([i], ctypes.c_char_p),
+        "gx_ctx_create": ([i, P(CtxOpts), P(vp)], i),
+        "gx_ctx_destroy": ([vp], None),
+        "gx_ctx_mark": ([vp, i], i),
+        "gx_ctx_elapsed_ms": ([vp, i, i, P(ctypes.c_double)], i),
+        "gx_ctx_synchronize": ([vp], i),
+        "gx_job_create": ([vp, P(JobOpts), P(vp)], i),
+        "gx_job_add_input": ([vp, vp, sz, i], i),
+        "gx_job_add_input_device": ([vp, vp, sz, i], i),
+        "gx_job_run": ([vp], i),
+        "gx_job_emit": ([vp, i, vp, sz, P(sz), P(i)], i),
+        "gx_job_records_device": ([vp, P(vp), P(sz), P(P(ctypes.c_uint64))], i),
+        "gx_job_stats": ([vp, P(Stats)], i),
+        "gx_job_destroy": ([vp], None),
+        "gx_batch_run": ([vp, P(vp), i, P(i)], i),
+        "gx_pinned_alloc": ([sz, P(vp)], i),
+        "gx_pinned_free": ([vp], None),
+        "gx_fastq_to_readid": ([vp, sz, vp, sz, P(vp), P(sz)], i),
+        "gx_host_free": ([vp], None),
+        "gx_seqfile_write": ([vp, sz, vp, ctypes.c_uint64, P(vp), P(sz)], i),
+        "gx_seqfile_read": ([vp, sz, P(vp), P(sz)], i),
+        "gx_records_to_text": ([vp, sz, P(vp), P(sz)], i),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def status_str(st):
+    return load().gx_status_str(st).decode()

@@ -1,0 +1,657 @@
+// gx_job.cu — contexts, jobs and the plain (one job per launch sequence) graph build.
+//
+// Run sequence of gx_job_run, all on the context's stream:
+//   K1   count + write line ends, parse lines, list valid mates     (host sync: line count,
+//        then errors + occurrence count, which sizes the table)
+//   K2/3 k-mer extraction and table inserts, one thread per read
+//   K4   read heads bucketed per table partition
+//   K5a  per-partition compaction, sort and sizing                  (host sync: output bytes)
+//   K5b  per-partition serialization
+// Device memory comes from the device's stream-ordered pool, kept warm between jobs.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gxgpu.h"
+#include "gx_host.h"
+#include "gx_kernels.cuh"
+
+using namespace gx;
+
+namespace {
+
+enum JobState { JS_INPUT = 0, JS_RAN = 1, JS_FAILED = 2 };
+
+struct Timers {
+    cudaEvent_t ev[10] = {};
+    bool ok = false;
+    void init() {
+        for (auto &e : ev)
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+        ok = true;
+    }
+    void destroy() {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    float ms(int a, int b) const {
+        float t = 0;
+        if (ok) cudaEventElapsedTime(&t, ev[a], ev[b]);
+        return t;
+    }
+};
+
+}  // namespace
+
+struct gx_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    size_t mem_limit = 0;
+    cudaEvent_t marks[16] = {};
+};
+
+struct gx_job {
+    gx_ctx *ctx = nullptr;
+    gx_job_opts o{};
+    int k = 0;
+    int wide = 0;
+    JobState state = JS_INPUT;
+    // readid input on the device
+    uint8_t *d_text = nullptr;
+    size_t text_len = 0, text_cap = 0;
+    bool text_borrowed = false;
+    int n_device_inputs = 0;
+    // FASTQ inputs kept on the host until run (mate stream 0 / 1, one entry per file)
+    std::vector<std::string> fastq[2];
+    // results
+    uint8_t *d_out = nullptr;
+    size_t out_bytes = 0;
+    uint32_t nparts = 0;
+    unsigned long long *d_part_off = nullptr;  // table-partition byte offsets (nparts + 1)
+    std::vector<uint64_t> part_bounds;         // output-part byte offsets (out_parts + 1)
+    std::vector<uint64_t> cursor;              // emit cursor per output part
+    std::vector<unsigned long long> h_part_off;  // lazily fetched copy of d_part_off
+    gx_stats st{};
+    Timers tm;
+};
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            fprintf(stderr, "gxgpu: %s failed: %s (%s:%d)\n", #call, cudaGetErrorString(e_), __FILE__, \
+                    __LINE__);                                                                      \
+            return e_ == cudaErrorMemoryAllocation ? GX_ENOMEM : GX_ECUDA;                          \
+        }                                                                                           \
+    } while (0)
+
+// Allocations of one run, released together (stream ordered).
+struct RunArena {
+    cudaStream_t s;
+    std::vector<void *> ptrs;
+    explicit RunArena(cudaStream_t st) : s(st) {}
+    template <class T>
+    gx_status alloc(T *&p, size_t count) {
+        void *q = nullptr;
+        const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+        cudaError_t e = cudaMallocAsync(&q, bytes, s);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return GX_ENOMEM;
+        }
+        ptrs.push_back(q);
+        p = (T *)q;
+        return GX_OK;
+    }
+    void release() {
+        for (void *p : ptrs) cudaFreeAsync(p, s);
+        ptrs.clear();
+    }
+    ~RunArena() { release(); }
+};
+
+static gx_status ensure_text_cap(gx_job *j, size_t need) {
+    if (j->text_borrowed) {
+        // switch a borrowed single input to an owned buffer before appending
+        uint8_t *old = j->d_text;
+        size_t cap = std::max<size_t>(need + 64, j->text_len * 2);
+        void *q = nullptr;
+        CK(cudaMallocAsync(&q, cap, j->ctx->stream));
+        CK(cudaMemcpyAsync(q, old, j->text_len, cudaMemcpyDeviceToDevice, j->ctx->stream));
+        j->d_text = (uint8_t *)q;
+        j->text_cap = cap;
+        j->text_borrowed = false;
+        return GX_OK;
+    }
+    if (need <= j->text_cap) return GX_OK;
+    size_t cap = std::max<size_t>(need + 64, j->text_cap * 2);
+    if (j->o.est_input_bytes > cap) cap = j->o.est_input_bytes + 64;
+    void *q = nullptr;
+    CK(cudaMallocAsync(&q, cap, j->ctx->stream));
+    if (j->d_text) {
+        CK(cudaMemcpyAsync(q, j->d_text, j->text_len, cudaMemcpyDeviceToDevice, j->ctx->stream));
+        cudaFreeAsync(j->d_text, j->ctx->stream);
+    }
+    j->d_text = (uint8_t *)q;
+    j->text_cap = cap;
+    return GX_OK;
+}
+
+// Appends one readid "file"; a file that does not end in '\n' gets one, so lines never
+// join across files ("...\r" + "\n" is a single CRLF terminator).
+static gx_status append_text(gx_job *j, const void *src, size_t bytes, cudaMemcpyKind kind, bool src_ends_nl) {
+    if (!bytes) return GX_OK;
+    const size_t add = bytes + (src_ends_nl ? 0 : 1);
+    gx_status st = ensure_text_cap(j, j->text_len + add);
+    if (st != GX_OK) return st;
+    CK(cudaMemcpyAsync(j->d_text + j->text_len, src, bytes, kind, j->ctx->stream));
+    if (!src_ends_nl) CK(cudaMemsetAsync(j->d_text + j->text_len + bytes, '\n', 1, j->ctx->stream));
+    j->text_len += add;
+    return GX_OK;
+}
+
+extern "C" {
+
+gx_status gx_pinned_alloc(size_t bytes, void **out) {
+    if (!out) return GX_EINVAL;
+    *out = nullptr;
+    if (cudaMallocHost(out, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        return GX_ENOMEM;
+    }
+    return GX_OK;
+}
+
+void gx_pinned_free(void *ptr) {
+    if (ptr) cudaFreeHost(ptr);
+}
+
+gx_status gx_ctx_create(int device, const gx_ctx_opts *opts, gx_ctx **out) {
+    if (!out) return GX_EINVAL;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        fprintf(stderr, "gxgpu: no CUDA device available\n");
+        return GX_ECUDA;
+    }
+    if (device < 0 || device >= n) return GX_EINVAL;
+    gx_ctx *c = new (std::nothrow) gx_ctx();
+    if (!c) return GX_ENOMEM;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) !=
+                                                    cudaSuccess) {
+        delete c;
+        return GX_ECUDA;
+    }
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = ~0ULL;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    c->mem_limit = (opts && opts->device_mem_limit) ? opts->device_mem_limit : (size_t)(0.9 * (double)fr);
+    for (auto &e : c->marks) cudaEventCreate(&e);
+    *out = c;
+    return GX_OK;
+}
+
+void gx_ctx_destroy(gx_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto &e : c->marks)
+        if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+gx_status gx_ctx_mark(gx_ctx *c, int slot) {
+    if (!c || slot < 0 || slot >= 16) return GX_EINVAL;
+    cudaSetDevice(c->device);
+    CK(cudaEventRecord(c->marks[slot], c->stream));
+    return GX_OK;
+}
+
+gx_status gx_ctx_elapsed_ms(gx_ctx *c, int a, int b, double *ms) {
+    if (!c || !ms || a < 0 || b < 0 || a >= 16 || b >= 16) return GX_EINVAL;
+    cudaSetDevice(c->device);
+    CK(cudaEventSynchronize(c->marks[b]));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, c->marks[a], c->marks[b]));
+    *ms = t;
+    return GX_OK;
+}
+
+gx_status gx_ctx_synchronize(gx_ctx *c) {
+    if (!c) return GX_EINVAL;
+    cudaSetDevice(c->device);
+    CK(cudaStreamSynchronize(c->stream));
+    return GX_OK;
+}
+
+gx_status gx_job_create(gx_ctx *c, const gx_job_opts *opts, gx_job **out) {
+    if (!c || !opts || !out) return GX_EINVAL;
+    *out = nullptr;
+    if (opts->kmer_length < 3 || opts->kmer_length > 64) return GX_EINVAL;
+    if (opts->input_kind != GX_INPUT_READID && opts->input_kind != GX_INPUT_FASTQ) return GX_EINVAL;
+    if (opts->out_parts < 0 || opts->load_factor < 0 || opts->load_factor > 0.95) return GX_EINVAL;
+    if (opts->max_readids_per_edge < 0) return GX_EINVAL;  // GenomixJobConf.validateConf :456-457
+    gx_job *j = new (std::nothrow) gx_job();
+    if (!j) return GX_ENOMEM;
+    j->ctx = c;
+    j->o = *opts;
+    if (j->o.out_parts == 0) j->o.out_parts = 1;
+    if (j->o.load_factor == 0) j->o.load_factor = 0.5;
+    j->k = opts->kmer_length;
+    j->wide = j->k > 32 ? 1 : 0;
+    cudaSetDevice(c->device);
+    j->tm.init();
+    *out = j;
+    return GX_OK;
+}
+
+gx_status gx_job_add_input(gx_job *j, const void *host, size_t bytes, int mate_stream) {
+    if (!j || (!host && bytes)) return GX_EINVAL;
+    if (j->state != JS_INPUT) return GX_ESTATE;
+    std::lock_guard<std::mutex> lk(j->ctx->mu);
+    cudaSetDevice(j->ctx->device);
+    if (j->o.input_kind == GX_INPUT_FASTQ) {
+        if (mate_stream < 0 || mate_stream > (j->o.paired ? 1 : 0)) return GX_EINVAL;
+        j->fastq[mate_stream].emplace_back((const char *)host, bytes);
+        return GX_OK;
+    }
+    if (mate_stream != 0) return GX_EINVAL;
+    const bool nl = bytes > 0 && ((const uint8_t *)host)[bytes - 1] == '\n';
+    gx_status st = append_text(j, host, bytes, cudaMemcpyHostToDevice, nl);
+    if (st != GX_OK) return st;
+    CK(cudaStreamSynchronize(j->ctx->stream));  // the host buffer is only borrowed for this call
+    return GX_OK;
+}
+
+gx_status gx_job_add_input_device(gx_job *j, const void *dev, size_t bytes, int mate_stream) {
+    if (!j || (!dev && bytes) || mate_stream != 0) return GX_EINVAL;
+    if (j->o.input_kind != GX_INPUT_READID) return GX_EINVAL;
+    if (((uintptr_t)dev & 15) != 0) return GX_EINVAL;
+    if (j->state != JS_INPUT) return GX_ESTATE;
+    if (!bytes) return GX_OK;
+    std::lock_guard<std::mutex> lk(j->ctx->mu);
+    cudaSetDevice(j->ctx->device);
+    if (j->text_len == 0 && j->n_device_inputs == 0) {
+        // a single device input is used in place; a missing final terminator is handled
+        // by the line kernels (a last line ends at the buffer end)
+        j->d_text = (uint8_t *)dev;
+        j->text_len = bytes;
+        j->text_cap = bytes;
+        j->text_borrowed = true;
+        j->n_device_inputs = 1;
+        return GX_OK;
+    }
+    uint8_t last = 0;
+    CK(cudaMemcpyAsync(&last, (const uint8_t *)dev + bytes - 1, 1, cudaMemcpyDeviceToHost, j->ctx->stream));
+    CK(cudaStreamSynchronize(j->ctx->stream));
+    if (j->text_borrowed && j->text_len) {
+        // make the borrowed first input end with a terminator before appending
+        uint8_t l0 = 0;
+        CK(cudaMemcpy(&l0, j->d_text + j->text_len - 1, 1, cudaMemcpyDeviceToHost));
+        gx_status st = ensure_text_cap(j, j->text_len + bytes + 2);
+        if (st != GX_OK) return st;
+        if (l0 != '\n') {
+            CK(cudaMemsetAsync(j->d_text + j->text_len, '\n', 1, j->ctx->stream));
+            j->text_len++;
+        }
+    }
+    j->n_device_inputs++;
+    return append_text(j, dev, bytes, cudaMemcpyDeviceToDevice, last == '\n');
+}
+
+static gx_status run_job(gx_job *j);
+
+gx_status gx_job_run(gx_job *j) {
+    if (!j) return GX_EINVAL;
+    if (j->state != JS_INPUT) return GX_ESTATE;
+    std::lock_guard<std::mutex> lk(j->ctx->mu);
+    cudaSetDevice(j->ctx->device);
+    const uint64_t l0 = launches_this_thread();
+    gx_status st = run_job(j);
+    j->st.kernel_launches = launches_this_thread() - l0;
+    j->state = st == GX_OK ? JS_RAN : JS_FAILED;
+    if (j->text_borrowed) {
+        j->d_text = nullptr;  // the caller's buffer is no longer referenced
+        j->text_borrowed = false;
+    }
+    return st;
+}
+
+gx_status gx_job_stats(const gx_job *j, gx_stats *out) {
+    if (!j || !out) return GX_EINVAL;
+    *out = j->st;
+    return GX_OK;
+}
+
+gx_status gx_job_records_device(gx_job *j, const void **dev, size_t *bytes, const uint64_t **part_offsets) {
+    if (!j || !dev || !bytes) return GX_EINVAL;
+    if (j->state != JS_RAN) return GX_ESTATE;
+    *dev = j->d_out;
+    *bytes = j->out_bytes;
+    if (part_offsets) *part_offsets = j->part_bounds.data();
+    return GX_OK;
+}
+
+gx_status gx_job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *written, int *more) {
+    if (!j || !written || !more || (!host_out && cap)) return GX_EINVAL;
+    if (j->state != JS_RAN) return GX_ESTATE;
+    if (part < 0 || part >= j->o.out_parts) return GX_EINVAL;
+    std::lock_guard<std::mutex> lk(j->ctx->mu);
+    cudaSetDevice(j->ctx->device);
+    const uint64_t end = j->part_bounds[part + 1];
+    uint64_t cur = j->cursor[part];
+    *written = 0;
+    *more = cur < end ? 1 : 0;
+    if (cur >= end || cap == 0) return GX_OK;
+    uint64_t stop = end;
+    if (end - cur > cap) {
+        // end on a record boundary: the last table-partition boundary that fits, else walk
+        // the records of the partition that straddles the limit
+        if (j->h_part_off.empty()) {
+            j->h_part_off.resize(j->nparts + 1);
+            CK(cudaMemcpy(j->h_part_off.data(), j->d_part_off, (j->nparts + 1) * sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost));
+        }
+        const uint64_t lim = cur + cap;
+        auto it = std::upper_bound(j->h_part_off.begin(), j->h_part_off.end(), (unsigned long long)lim);
+        uint64_t b = (it == j->h_part_off.begin()) ? 0 : *(it - 1);
+        if (b > cur) {
+            stop = b;
+        } else {
+            CK(cudaMemcpy(host_out, j->d_out + cur, cap, cudaMemcpyDeviceToHost));
+            const uint8_t *h = (const uint8_t *)host_out;
+            uint64_t p = 0;
+            while (p + 8 <= cap) {
+                const uint32_t rl = ((uint32_t)h[p] << 24) | ((uint32_t)h[p + 1] << 16) | ((uint32_t)h[p + 2] << 8) |
+                                    h[p + 3];
+                if (p + 8 + rl > cap) break;
+                p += 8 + rl;
+            }
+            if (p == 0) return GX_EINVAL;  // one record is larger than the buffer
+            j->cursor[part] = cur + p;
+            *written = p;
+            *more = cur + p < end ? 1 : 0;
+            return GX_OK;
+        }
+    }
+    CK(cudaMemcpyAsync(host_out, j->d_out + cur, stop - cur, cudaMemcpyDeviceToHost, j->ctx->stream));
+    CK(cudaStreamSynchronize(j->ctx->stream));
+    j->cursor[part] = stop;
+    *written = stop - cur;
+    *more = stop < end ? 1 : 0;
+    return GX_OK;
+}
+
+void gx_job_destroy(gx_job *j) {
+    if (!j) return;
+    {
+        std::lock_guard<std::mutex> lk(j->ctx->mu);
+        cudaSetDevice(j->ctx->device);
+        cudaStream_t s = j->ctx->stream;
+        if (j->d_text && !j->text_borrowed) cudaFreeAsync(j->d_text, s);
+        if (j->d_out) cudaFreeAsync(j->d_out, s);
+        if (j->d_part_off) cudaFreeAsync(j->d_part_off, s);
+        cudaStreamSynchronize(s);
+        j->tm.destroy();
+    }
+    delete j;
+}
+
+gx_status gx_batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses) {
+    if (!c || (!jobs && n) || n < 0) return GX_EINVAL;
+    gx_status first = GX_OK;
+    for (int i = 0; i < n; i++) {
+        gx_status s = jobs[i] && jobs[i]->ctx == c ? gx_job_run(jobs[i]) : GX_EINVAL;
+        if (statuses) statuses[i] = s;
+        if (s != GX_OK && first == GX_OK) first = s;
+    }
+    return first;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// the run
+// ---------------------------------------------------------------------------------------
+static gx_status run_job(gx_job *j) {
+    cudaStream_t s = j->ctx->stream;
+    Timers &tm = j->tm;
+    memset(&j->st, 0, sizeof j->st);
+    j->st.key_bits = j->wide ? 128 : 64;
+    const int k = j->k;
+
+    // FASTQ: the reference driver's conversion, then the readid path
+    if (j->o.input_kind == GX_INPUT_FASTQ) {
+        const size_t nf = j->fastq[0].size();
+        if (j->o.paired && j->fastq[1].size() != nf) return GX_EFASTQ_PAIRING;
+        for (size_t f = 0; f < nf; f++) {
+            std::string txt;
+            const std::string &a = j->fastq[0][f];
+            const std::string *b = j->o.paired ? &j->fastq[1][f] : nullptr;
+            gx_status st = gxh::fastq_to_readid((const uint8_t *)a.data(), a.size(),
+                                                b ? (const uint8_t *)b->data() : nullptr, b ? b->size() : 0, txt);
+            if (st != GX_OK) return st;
+            st = append_text(j, txt.data(), txt.size(), cudaMemcpyHostToDevice, true);
+            if (st != GX_OK) return st;
+            CK(cudaStreamSynchronize(s));
+        }
+        j->fastq[0].clear();
+        j->fastq[1].clear();
+    }
+
+    const uint64_t n_text = j->text_len;
+    const uint8_t *text = j->d_text;
+    j->part_bounds.assign(j->o.out_parts + 1, 0);
+    j->cursor.assign(j->o.out_parts, 0);
+    if (n_text == 0) return GX_OK;
+
+    RunArena ar(s);
+    DevStatus *d_st;
+    gx_status e;
+    if ((e = ar.alloc(d_st, 1)) != GX_OK) return e;
+    {
+        DevStatus init{};
+        init.parse_err = ~0ULL;
+        CK(cudaMemcpyAsync(d_st, &init, sizeof init, cudaMemcpyHostToDevice, s));
+    }
+    const uint64_t tiles = line_tiles(n_text);
+    uint32_t *tile_cnt, *d_nlines;
+    void *scratch;
+    const size_t scratch_bytes = std::max(scan_scratch_bytes(std::max<uint64_t>(tiles, 1), 8),
+                                          scan_scratch_bytes(n_text + 16, 8));
+    if ((e = ar.alloc(tile_cnt, tiles + 1)) != GX_OK) return e;
+    if ((e = ar.alloc(d_nlines, 4)) != GX_OK) return e;
+    if ((e = ar.alloc(scratch, scratch_bytes)) != GX_OK) return e;
+
+    // ---- K1 ----
+    CK(cudaEventRecord(tm.ev[0], s));
+    launch_count_lines(text, n_text, tile_cnt, s);
+    exclusive_scan_u32(tile_cnt, tile_cnt, tiles, d_nlines, scratch, s);
+    uint32_t n_lines = 0;
+    CK(cudaMemcpyAsync(&n_lines, d_nlines, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    j->st.lines = n_lines;
+    unsigned long long *line_end;
+    LineRec *lines;
+    uint8_t *lflags;
+    uint32_t *nvalid, *reads;
+    if ((e = ar.alloc(line_end, n_lines)) != GX_OK) return e;
+    if ((e = ar.alloc(lines, n_lines)) != GX_OK) return e;
+    if ((e = ar.alloc(lflags, n_lines)) != GX_OK) return e;
+    if ((e = ar.alloc(nvalid, n_lines)) != GX_OK) return e;
+    if ((e = ar.alloc(reads, 2ull * n_lines)) != GX_OK) return e;
+    launch_write_lines(text, n_text, tile_cnt, line_end, s);
+    launch_parse_lines(text, n_text, line_end, n_lines, k, lines, lflags, nvalid, d_st, s);
+    exclusive_scan_u32(nvalid, nvalid, n_lines, d_nlines + 1, scratch, s);
+    launch_read_list(lflags, nvalid, lines, n_lines, k, reads, d_st, s);
+    CK(cudaEventRecord(tm.ev[1], s));
+    DevStatus hs;
+    uint32_t n_reads = 0;
+    CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&n_reads, d_nlines + 1, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    if (hs.parse_err != ~0ULL) {
+        j->st.error_line = (hs.parse_err >> 8) + 1;
+        return (gx_status)(hs.parse_err & 0xff);
+    }
+    j->st.reads = n_reads;
+    j->st.kmers = hs.n_occ;
+    j->st.ms_parse = tm.ms(0, 1);
+    if (n_reads == 0) {
+        j->st.ms_total = tm.ms(0, 1);
+        return GX_OK;
+    }
+
+    // ---- table ----
+    const size_t slot_bytes = j->wide ? sizeof(Slot128) : sizeof(Slot64);
+    double lf = j->o.load_factor;
+    for (int attempt = 0;; attempt++) {
+        const uint64_t want = (uint64_t)((double)hs.n_occ / lf) + 1;
+        const uint64_t nparts64 = std::max<uint64_t>(1, (want + PART_SLOTS - 1) / PART_SLOTS);
+        if (nparts64 > 0x7fffffffULL) return GX_ENOMEM;
+        const uint32_t nparts = (uint32_t)nparts64;
+        const size_t table_bytes = (size_t)nparts * PART_SLOTS * slot_bytes;
+        if (table_bytes > j->ctx->mem_limit) return GX_ENOMEM;
+        RunArena tar(s);
+        void *table;
+        Head *heads;
+        uint32_t *head_cnt, *head_off, *head_cur, *head_idx, *head_cnt2, *part_nodes;
+        unsigned long long *head_sk, *part_bytes, *part_off;
+        if ((e = tar.alloc(table, table_bytes / 16 * 16 + 16)) != GX_OK) return e;
+        if ((e = tar.alloc(heads, n_reads)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cnt, nparts)) != GX_OK) return e;
+        if ((e = tar.alloc(head_off, nparts)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cur, nparts)) != GX_OK) return e;
+        if ((e = tar.alloc(head_idx, n_reads)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cnt2, nparts)) != GX_OK) return e;
+        if ((e = tar.alloc(head_sk, n_reads)) != GX_OK) return e;
+        if ((e = tar.alloc(part_nodes, nparts)) != GX_OK) return e;
+        if ((e = tar.alloc(part_bytes, nparts)) != GX_OK) return e;
+        void *pscratch;
+        if ((e = tar.alloc(pscratch, scan_scratch_bytes(nparts, 8))) != GX_OK) return e;
+        void *part_off_v = nullptr;
+        CK(cudaMallocAsync(&part_off_v, (nparts + 1) * sizeof(unsigned long long), s));
+        part_off = (unsigned long long *)part_off_v;
+
+        TableGeom g{table, nparts, j->wide};
+        CK(cudaMemsetAsync(table, 0, table_bytes, s));
+        CK(cudaMemsetAsync(head_cnt, 0, nparts * 4, s));
+        CK(cudaMemsetAsync(head_cur, 0, nparts * 4, s));
+        // ---- K2/K3 ----
+        CK(cudaEventRecord(tm.ev[2], s));
+        launch_insert(g, text, lines, reads, n_reads, k, heads, head_cnt, d_st, s);
+        CK(cudaEventRecord(tm.ev[3], s));
+        // ---- K4 + K5a ----
+        exclusive_scan_u32(head_cnt, head_off, nparts, nullptr, pscratch, s);
+        launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, nparts, s);
+        EmitArgs a{};
+        a.g = g;
+        a.k = k;
+        a.text = text;
+        a.lines = lines;
+        a.reads = reads;
+        a.heads = heads;
+        a.head_idx = head_idx;
+        a.head_sk = head_sk;
+        a.head_off = head_off;
+        a.head_cnt = head_cnt;
+        a.head_cnt2 = head_cnt2;
+        a.part_nodes = part_nodes;
+        a.part_bytes = part_bytes;
+        a.part_off = part_off;
+        a.st = d_st;
+        launch_emit_prepare(a, s);
+        exclusive_scan_u64(part_bytes, part_off, nparts, part_off + nparts, pscratch, s);
+        CK(cudaEventRecord(tm.ev[4], s));
+        unsigned long long total = 0;
+        CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&total, part_off + nparts, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaGetLastError());
+        if (hs.table_full) {
+            cudaFreeAsync(part_off, s);
+            // the upper bound on distinct k-mers is the occurrence count; a full partition
+            // means a skewed hash bucket, so retry with more slots
+            DevStatus zero{};
+            zero.parse_err = ~0ULL;
+            zero.n_reads = hs.n_reads;
+            zero.n_occ = hs.n_occ;
+            CK(cudaMemcpyAsync(d_st, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
+            if (attempt >= 2) return GX_ETABLE_FULL;
+            lf *= 0.5;
+            continue;
+        }
+        // ---- K5b ----
+        void *outp = nullptr;
+        CK(cudaMallocAsync(&outp, total + 16, s));
+        if (((uintptr_t)outp & 15) != 0) {  // the record writer stores aligned 16-byte vectors
+            cudaFreeAsync(outp, s);
+            cudaFreeAsync(part_off, s);
+            return GX_ECUDA;
+        }
+        a.out = (uint8_t *)outp;
+        CK(cudaEventRecord(tm.ev[5], s));
+        launch_emit_write(a, s);
+        CK(cudaEventRecord(tm.ev[6], s));
+        CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaGetLastError());
+        if (hs.internal_err) {
+            cudaFreeAsync(outp, s);
+            cudaFreeAsync(part_off, s);
+            fprintf(stderr, "gxgpu: internal error: record sizes disagree between emission passes\n");
+            return GX_ECUDA;
+        }
+        // output parts = contiguous ranges of table partitions
+        const int P = j->o.out_parts;
+        for (int q = 0; q <= P; q++) {
+            const uint64_t tp = (uint64_t)nparts * q / P;
+            unsigned long long v = 0;
+            if (q == P)
+                v = total;
+            else if (tp > 0)
+                CK(cudaMemcpy(&v, part_off + tp, 8, cudaMemcpyDeviceToHost));
+            j->part_bounds[q] = v;
+        }
+        // node and read-head totals
+        {
+            std::vector<uint32_t> pn(nparts), hc(nparts);
+            CK(cudaMemcpy(pn.data(), part_nodes, nparts * 4, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(hc.data(), head_cnt2, nparts * 4, cudaMemcpyDeviceToHost));
+            uint64_t nn = 0, nh = 0;
+            for (uint32_t q = 0; q < nparts; q++) {
+                nn += pn[q];
+                nh += hc[q];
+            }
+            j->st.nodes = nn;
+            j->st.read_heads = nh;
+        }
+        j->d_out = (uint8_t *)outp;
+        j->out_bytes = total;
+        j->d_part_off = part_off;
+        j->nparts = nparts;
+        j->st.record_bytes = total;
+        j->st.table_slots = (uint64_t)nparts * PART_SLOTS;
+        j->st.table_partitions = nparts;
+        j->st.max_probe = hs.max_probe;
+        j->st.cov_inexact_nodes = hs.cov_inexact;
+        j->st.ms_insert = tm.ms(2, 3);
+        j->st.ms_emit = tm.ms(3, 4) + tm.ms(5, 6);
+        j->st.ms_total = tm.ms(0, 6);
+        break;
+    }
+    return GX_OK;
+}

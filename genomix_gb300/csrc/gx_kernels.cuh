@@ -1,0 +1,78 @@
+// gx_kernels.cuh — declarations of the graph-build kernels and their host launchers.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gx_device.cuh"
+
+namespace gx {
+
+// ---- geometry ---------------------------------------------------------------------------
+constexpr int LINE_TILE_THREADS = 256;
+constexpr int LINE_TILE_VECS = 4;  // uint4 per thread
+constexpr uint64_t LINE_TILE_BYTES = (uint64_t)LINE_TILE_THREADS * LINE_TILE_VECS * 16;
+
+constexpr int PART_SLOTS_LOG2 = 11;  // slots per table partition (both key widths)
+constexpr uint32_t PART_SLOTS = 1u << PART_SLOTS_LOG2;
+constexpr int EMIT_THREADS = 256;
+constexpr uint32_t HEAD_CAP = 1024;         // read heads per partition sorted in shared memory
+constexpr uint32_t EMIT_STAGE_BYTES = 24576;  // output staging window per partition CTA
+
+// Kernel launches made by the calling host thread (read before and after a run).
+uint64_t launches_this_thread();
+
+// ---- scans (device-wide, exclusive) -----------------------------------------------------
+// Scratch needed by exclusive_scan for n items of T.
+size_t scan_scratch_bytes(uint64_t n, size_t elem);
+// out[i] = sum(in[0..i)); total (device pointer, may be null) = sum(in[0..n)).  in == out allowed.
+void exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint64_t n, uint32_t *total, void *scratch,
+                        cudaStream_t s);
+void exclusive_scan_u64(const unsigned long long *in, unsigned long long *out, uint64_t n,
+                        unsigned long long *total, void *scratch, cudaStream_t s);
+
+// ---- parse ------------------------------------------------------------------------------
+uint64_t line_tiles(uint64_t n_text);
+void launch_count_lines(const uint8_t *text, uint64_t n, uint32_t *tile_cnt, cudaStream_t s);
+void launch_write_lines(const uint8_t *text, uint64_t n, const uint32_t *tile_off, unsigned long long *line_end,
+                        cudaStream_t s);
+void launch_parse_lines(const uint8_t *text, uint64_t n_text, const unsigned long long *line_end, uint32_t n_lines,
+                        int k, LineRec *lines, uint8_t *lflags, uint32_t *nvalid, DevStatus *st, cudaStream_t s);
+void launch_read_list(const uint8_t *lflags, const uint32_t *read_off, const LineRec *lines, uint32_t n_lines, int k,
+                      uint32_t *reads, DevStatus *st, cudaStream_t s);
+
+// ---- build ------------------------------------------------------------------------------
+struct TableGeom {
+    void *table;        // Slot64[] or Slot128[]
+    uint32_t nparts;    // partitions
+    int wide;           // 0: 64-bit keys, 1: 128-bit keys
+};
+void launch_insert(const TableGeom &g, const uint8_t *text, const LineRec *lines, const uint32_t *reads,
+                   uint32_t n_reads, int k, Head *heads, uint32_t *head_cnt, DevStatus *st, cudaStream_t s);
+void launch_head_scatter(const Head *heads, uint32_t n_reads, const uint32_t *head_off, uint32_t *head_cur,
+                         uint32_t *head_idx, uint32_t nparts, cudaStream_t s);
+
+// ---- emission ---------------------------------------------------------------------------
+struct EmitArgs {
+    TableGeom g;
+    int k;
+    const uint8_t *text;
+    const LineRec *lines;
+    const uint32_t *reads;
+    Head *heads;
+    uint32_t *head_idx;          // read ordinals bucketed by partition, sorted in place
+    unsigned long long *head_sk; // scratch sort keys for partitions above HEAD_CAP
+    const uint32_t *head_off;
+    const uint32_t *head_cnt;
+    uint32_t *head_cnt2;         // heads kept after de-duplication
+    uint32_t *part_nodes;
+    unsigned long long *part_bytes;
+    const unsigned long long *part_off;
+    uint8_t *out;
+    DevStatus *st;
+};
+void launch_emit_prepare(const EmitArgs &a, cudaStream_t s);
+void launch_emit_write(const EmitArgs &a, cudaStream_t s);
+
+}  // namespace gx

@@ -104,6 +104,7 @@ typedef struct gx_stats {
     uint64_t cov_inexact_nodes; /* nodes with count >= 2^24 (float coverage no longer exact) */
     uint32_t max_probe;       /* longest probe sequence seen during inserts */
     uint32_t key_bits;        /* 64 or 128 */
+    uint64_t kernel_launches; /* kernels launched by gx_job_run */
     double ms_parse;          /* device time of the parse kernels */
     double ms_insert;         /* device time of k-mer extraction + table inserts */
     double ms_emit;           /* device time of compaction + record serialization */
@@ -116,6 +117,13 @@ typedef struct gx_stats {
  * the Hyracks cluster controller made in GenomixHyracksDriver.java:70-78. */
 gx_status gx_ctx_create(int device, const gx_ctx_opts *opts, gx_ctx **out);
 void gx_ctx_destroy(gx_ctx *ctx);
+
+/* Device-side timing on the context's stream: gx_ctx_mark records event `slot` (0..15),
+ * gx_ctx_elapsed_ms waits for event b and returns the time from a to b. */
+gx_status gx_ctx_mark(gx_ctx *ctx, int slot);
+gx_status gx_ctx_elapsed_ms(gx_ctx *ctx, int a, int b, double *ms);
+/* Wait until all work submitted on the context has finished. */
+gx_status gx_ctx_synchronize(gx_ctx *ctx);
 
 /* ---- plain (one job per launch sequence) ---------------------------------------------- */
 

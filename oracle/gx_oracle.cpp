@@ -709,7 +709,7 @@ static void group_sorted(size_t n, KeyAt key_at, ValAt val_at, Emit emit) {
         }
         std::string v;
         write_node(v, acc);
-        emit(std::string((const char *)kp, kl), std::move(v));
+        emit(std::string((const char *)kp, kl), std::move(v), acc);
         i = j;
     }
 }
@@ -772,7 +772,7 @@ static Result build(const uint8_t *text, size_t n, int k, int threads, int parts
                 p = ts.val(idx[i]);
                 l = ts.t[idx[i]].vlen;
             },
-            [&](std::string &&key, std::string &&val) {
+            [&](std::string &&key, std::string &&val, const Node &) {
                 int p = kmer_partition((const uint8_t *)key.data(), (int)key.size(), P);
                 routed[t][p].push_back(Grouped{std::move(key), std::move(val)});
             });
@@ -799,7 +799,7 @@ static Result build(const uint8_t *text, size_t n, int k, int threads, int parts
     // global stage: merge the sorted runs of each partition (M:N partitioning-merging
     // connector), group again, write the part
     res.parts.assign(P, std::string());
-    std::vector<uint64_t> p_nodes(P, 0);
+    std::vector<uint64_t> p_nodes(P, 0), p_heads(P, 0);
     auto global = [&](int p) {
         std::vector<const Grouped *> items;
         for (int t = 0; t < T; t++)
@@ -819,9 +819,10 @@ static Result build(const uint8_t *text, size_t n, int k, int threads, int parts
                 vp = (const uint8_t *)items[i]->val.data();
                 l = items[i]->val.size();
             },
-            [&](std::string &&key, std::string &&val) {
+            [&](std::string &&key, std::string &&val, const Node &acc) {
                 append_record(o, k, key, val);
                 p_nodes[p]++;
+                p_heads[p] += acc.unflipped.size() + acc.flipped.size();
             });
     };
     {
@@ -831,6 +832,8 @@ static Result build(const uint8_t *text, size_t n, int k, int threads, int parts
         for (auto &x : th) x.join();
     }
     for (auto v : p_nodes) res.nodes += v;
+    res.heads = 0;  // read heads in the output (TreeSet de-duplicates equal uuids)
+    for (auto v : p_heads) res.heads += v;
     return res;
 }
 

@@ -1,0 +1,79 @@
+"""The C ABI library on the CPU: it loads, exports every declared symbol, and its host-side
+formats agree with the oracle.  No kernel runs here."""
+import os
+import re
+
+import pytest
+
+from conftest import ROOT, golden_cases, golden_expected, golden_input
+from genomix_gb300 import _lib, build as gbuild
+import genomix_gb300 as gx
+from oracle import gx_oracle as go
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    gbuild.build()
+    return _lib.load()
+
+
+def declared_symbols():
+    with open(os.path.join(ROOT, "include", "gxgpu.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gx_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(built):
+    names = declared_symbols()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(built, n), n
+    assert sorted(_lib.EXPORTS) == names
+
+
+def test_status_strings(built):
+    for code, name in _lib.STATUS_NAMES.items():
+        assert _lib.status_str(code)
+    assert "kmersize" in _lib.status_str(5)
+
+
+def test_context_fails_loudly_without_gpu():
+    if os.path.exists("/dev/nvidia0"):
+        pytest.skip("GPU present")
+    with pytest.raises(gx.GraphBuildError) as e:
+        gx.Context(0)
+    assert e.value.name == "GX_ECUDA"
+
+
+def test_fastq_conversion_matches_oracle():
+    fq1 = b"@a\nACGTAC\n+\nIIIIII\n@b\n\tGGCATT \r\n+\nIIIIII\n@c\nAC\n+\nII"
+    fq2 = b"@a\nTTTGCA\n+\nIIIIII\n@b\nCCCGGA\n+\nIIIIII\n@c\nGG\n+\nII"
+    assert gx.fastq_to_readid(fq1, fq2) == go.fastq_to_readid(fq1, fq2)[1]
+    assert gx.fastq_to_readid(fq1) == go.fastq_to_readid(fq1)[1]
+    with pytest.raises(gx.GraphBuildError) as e:
+        gx.fastq_to_readid(fq1, fq2 + b"\n@d\n")
+    assert e.value.name == "GX_EFASTQ_PAIRING"
+
+
+@pytest.mark.parametrize("case", golden_cases(), ids=[c["name"] for c in golden_cases()])
+def test_product_text_dump_matches_golden(case):
+    """The library's text dump of oracle records equals the reference's dump form."""
+    res = go.build_graph(golden_input(case["name"]), case["k"], threads=2, parts=4)
+    assert gx.records_to_text(res.records) == go.dump_text(res.records)
+
+
+def test_seqfile_round_trip_and_header():
+    from genomix_gb300 import synth
+    text = synth.small_random(3, 300, 80, 21, paired=True)
+    res = go.build_graph(text, 21)
+    f = gx.seqfile_write(res.records, seed=5)
+    assert f[:4] == b"SEQ\x06"
+    assert b"edu.uci.ics.genomix.data.types.VKmer" in f[:100]
+    assert b"edu.uci.ics.genomix.data.types.Node" in f[:100]
+    assert gx.seqfile_read(f) == res.records
+    # sync escapes appear roughly every 2000 bytes
+    assert f.count(b"\xff\xff\xff\xff" + f[f.index(b"Node") + 4 + 6:f.index(b"Node") + 4 + 6 + 16]) >= len(
+        res.records) // 2200
+    assert gx.seqfile_write(res.records, seed=5) == f  # deterministic sync marker
+    assert gx.seqfile_write(res.records, seed=6) != f

@@ -1,0 +1,227 @@
+"""GPU graph build vs the oracle and the reference's golden fixtures, through the C ABI.
+
+Bit-exact: the comparison form is the sorted set of records with every edge list sorted
+(the reference's own test treats the edge lists as unordered, BatchTestFilesTest.java:171);
+record bytes, read-head order and coverage are compared exactly.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, golden_expected, golden_input
+import genomix_gb300 as gx
+from genomix_gb300 import synth
+from oracle import gx_oracle as go
+import refcompare
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = gx.Context(0)
+    yield c
+    c.close()
+
+
+def gpu_build(ctx, text, k, **kw):
+    job = gx.GraphBuildJob(ctx, k, **kw)
+    job.add_input(text)
+    job.run()
+    rec = job.records()
+    st = job.stats()
+    job.close()
+    return rec, st
+
+
+def assert_same(ctx, text, k, threads=2, parts=3, **kw):
+    rec, st = gpu_build(ctx, text, k, **kw)
+    ref = go.build_graph(text, k, threads=threads, parts=parts)
+    assert ref.status == 0
+    assert st["nodes"] == ref.nodes
+    assert st["kmers"] == ref.kmers
+    assert st["reads"] == ref.reads
+    assert st["read_heads"] == ref.read_heads
+    assert go.normalize(rec) == go.normalize(ref.records)
+    return rec, st
+
+
+@pytest.mark.parametrize("case", golden_cases(), ids=[c["name"] for c in golden_cases()])
+def test_golden_fixtures(ctx, case):
+    rec, _ = gpu_build(ctx, golden_input(case["name"]), case["k"])
+    text = gx.records_to_text(rec)
+    exp = golden_expected(case["name"])
+    refcompare.compare_unordered(exp, text)
+    assert refcompare.strict_normal_form(text) == refcompare.strict_normal_form(exp)
+
+
+@pytest.mark.parametrize("k", [3, 4, 5, 8, 15, 16, 21, 31, 32, 33, 36, 47, 55, 63, 64])
+def test_random_single_end_all_k(ctx, k):
+    text = synth.small_random(100 + k, 300, max(k + 20, 70), k, genome_len=1500, err=0.02)
+    assert_same(ctx, text, k)
+
+
+@pytest.mark.parametrize("k", [21, 31, 55])
+def test_random_paired_with_n(ctx, k):
+    text = synth.small_random(200 + k, 400, 150, k, paired=True, genome_len=5000, err=0.01, n_rate=0.003)
+    assert_same(ctx, text, k)
+
+
+def test_palindromes_even_k(ctx):
+    # tandem palindromic sequence: every k-mer for even k is close to its own reverse complement
+    unit = b"ACGT" * 10 + b"AATT" * 10 + b"GGCC" * 5
+    lines = [b"%d\t%s" % (4 * i + 2, unit[i % 7:] + unit[: i % 5]) for i in range(50)]
+    text = b"\n".join(lines) + b"\n"
+    for k in (4, 6, 8, 10):
+        assert_same(ctx, text, k)
+
+
+def test_high_multiplicity_repeats(ctx):
+    # one 40-base unit repeated: few nodes with very high coverage and many read heads
+    rng = np.random.default_rng(5)
+    unit = "".join(rng.choice(list("ACGT"), 40))
+    genome = unit * 60
+    lines = []
+    for i in range(3000):
+        s = int(rng.integers(0, len(genome) - 120))
+        lines.append(f"{4 * i + 2}\t{genome[s:s + 100]}\t{genome[s + 10:s + 110]}")
+    text = ("\n".join(lines) + "\n").encode()
+    rec, st = assert_same(ctx, text, 21)
+    assert st["read_heads"] == 6000 or st["read_heads"] < 6000  # heads merge into few nodes
+
+
+def test_many_heads_one_partition(ctx):
+    # every read starts with the same k-mer: one node carries > 1024 read heads
+    rng = np.random.default_rng(9)
+    prefix = "ACGTTGCAAGGCTTCA"
+    lines = []
+    for i in range(2500):
+        tail = "".join(rng.choice(list("ACGT"), 30))
+        lines.append(f"{i}\t{prefix}{tail}")
+    text = ("\n".join(lines) + "\n").encode()
+    rec, st = assert_same(ctx, text, 11)
+
+
+def test_duplicate_read_ids(ctx):
+    text = b"5\tACGTACGTAC\n5\tACGTACGTAC\n5\tACGTACGGGC\n7\tACGTACGTAC\n"
+    assert_same(ctx, text, 5)
+
+
+def test_lowercase_crlf_and_missing_final_newline(ctx):
+    text = b"1\tacgtacGGTA\r\n2\tGGCATTaCCA\t\tx\r3\tTTGACCAGTA\tACGNNAC\n4\tCCCCGGGGAA"
+    ref = go.build_graph(text, 5)
+    assert ref.status == 2  # line 2 has 4 fields
+    with pytest.raises(gx.GraphBuildError):
+        gpu_build(ctx, text, 5)
+    text = b"1\tacgtacGGTA\r\n2\tGGCATTaCCA\t\t\r3\tTTGACCAGTA\tACGNNAC\n4\tCCCCGGGGAA"
+    assert_same(ctx, text, 5)
+
+
+@pytest.mark.parametrize("text,status,line", [
+    (b"1\tACGTACG\n2\n", "GX_EINVAL_LINE", 2),
+    (b"1\tACGTA\tCC\tGG\n", "GX_EINVAL_LINE", 1),
+    (b"x\tACGTA\n", "GX_EINVAL_NUMBER", 1),
+    (b"1\tACGTA\n+\tAC\n", "GX_EINVAL_NUMBER", 2),
+    (b"99999999999999999999\tACGTA\n", "GX_EINVAL_NUMBER", 1),
+    (b"-1\tACGTA\n", "GX_EREADID_RANGE", 1),
+    (b"34359738368\tACGTA\n", "GX_EREADID_RANGE", 1),
+    (b"1\tACGTAC\n2\tACG\n", "GX_EREAD_TOO_SHORT", 2),
+    (b"1\tACGTAC\n2\tACGTAC\tACG\n", "GX_EREAD_TOO_SHORT", 2),
+    (b"1\tACGTAC\n\n3\tACGTAC\n", "GX_EINVAL_LINE", 2),
+    (b"1\tACGTAC\n2\tAC\n3\t\n", "GX_EREAD_TOO_SHORT", 2),
+])
+def test_parse_errors(ctx, text, status, line):
+    ref = go.build_graph(text, 3)
+    assert gx._lib.STATUS_NAMES[ref.status] == status and ref.error_line == line
+    with pytest.raises(gx.GraphBuildError) as e:
+        gpu_build(ctx, text, 3)
+    assert e.value.name == status
+    assert e.value.line == line
+
+
+def test_invalid_mates_and_unchecked_read_id(ctx):
+    # no valid mate: the read id is never range-checked; N drops the whole mate
+    text = b"34359738368\tNNNN\n2\tACGNT\tACGTTA\n3\t\tACGTTGCA\n"
+    assert_same(ctx, text, 3)
+
+
+def test_empty_input(ctx):
+    job = gx.GraphBuildJob(ctx, 21)
+    job.run()
+    assert job.records() == b""
+    assert job.stats()["nodes"] == 0
+    job.close()
+    rec, st = gpu_build(ctx, b"1\tNNNNNNNNNNNNNNNNNNNNNN\n", 5)
+    assert rec == b"" and st["nodes"] == 0
+
+
+def test_multiple_inputs_and_parts(ctx):
+    a = synth.small_random(11, 200, 80, 21)
+    b = synth.small_random(12, 200, 80, 21)
+    job = gx.GraphBuildJob(ctx, 21, out_parts=4)
+    job.add_input(a[:-1])  # a file without its final newline
+    job.add_input(b)
+    job.run()
+    parts = [job.records(q) for q in range(4)]
+    whole = job.records()
+    assert b"".join(parts) == whole
+    chunked = job.records(2, chunk=500)
+    assert chunked == parts[2]
+    job.close()
+    ref = go.build_graph(a + b, 21)
+    assert go.normalize(whole) == go.normalize(ref.records)
+
+
+def test_device_input(ctx):
+    torch = pytest.importorskip("torch")
+    text = synth.small_random(21, 500, 120, 31, paired=True, genome_len=4000)
+    t = torch.frombuffer(bytearray(text), dtype=torch.uint8).cuda()
+    job = gx.GraphBuildJob(ctx, 31)
+    job.add_input_device(t.data_ptr(), t.numel(), keepalive=t)
+    job.run()
+    rec = job.records()
+    job.close()
+    ref = go.build_graph(text, 31)
+    assert go.normalize(rec) == go.normalize(ref.records)
+
+
+def test_fastq_input(ctx):
+    rng = np.random.default_rng(4)
+    n, L = 300, 90
+    g = "".join(rng.choice(list("ACGT"), 3000))
+    fq1, fq2 = [], []
+    for i in range(n):
+        s = int(rng.integers(0, 2800))
+        fq1.append(f"@r{i}\n{g[s:s + L]}\n+\n{'?' * L}\n")
+        fq2.append(f"@r{i}\n{g[s + 50:s + 50 + L]}\n+\n{'?' * L}\n")
+    f1, f2 = "".join(fq1).encode(), "".join(fq2).encode()
+    job = gx.GraphBuildJob(ctx, 21, input_kind="fastq", paired=True)
+    job.add_input(f1, 0)
+    job.add_input(f2, 1)
+    job.run()
+    rec = job.records()
+    job.close()
+    ref = go.build_graph(go.fastq_to_readid(f1, f2)[1], 21)
+    assert go.normalize(rec) == go.normalize(ref.records)
+
+
+def test_deterministic_output(ctx):
+    text = synth.small_random(31, 2000, 150, 31, paired=True, genome_len=20000)
+    a, _ = gpu_build(ctx, text, 31)
+    b, _ = gpu_build(ctx, text, 31)
+    assert a == b
+
+
+def test_low_load_factor_and_retry(ctx):
+    text = synth.small_random(41, 500, 100, 21, genome_len=30000, err=0.05)
+    assert_same(ctx, text, 21, load_factor=0.9)
+
+
+def test_medium_case_against_oracle(ctx):
+    w = synth.pe_5mbp(max_pairs=20000, genome_len=200_000)
+    assert_same(ctx, w.text, 31, threads=4, parts=4)
+
+
+def test_seqfile_of_gpu_records(ctx):
+    text = synth.small_random(51, 300, 100, 21, paired=True)
+    rec, _ = gpu_build(ctx, text, 21)
+    assert gx.seqfile_read(gx.seqfile_write(rec, seed=1)) == rec
