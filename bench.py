@@ -35,7 +35,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "k-mers/s, bit-exact graph build, batched vs per-job, 1 GB300; p99 job latency"
 UNIT = "k-mers/s"
-CPU_SAMPLE_PAIRS = 120_000
+CPU_SAMPLE_PAIRS = 120_000   # cpu_baseline sample (one run)
+REF_STEP_PAIRS = 60_000      # --impl reference: sample per step
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_insert_pe5mbp_ncu.txt")
 
 
@@ -167,10 +168,10 @@ def run_reference(args, ws, rank):
     if rank != 0:
         return
     w = workload(args.max_pairs)
-    sample = sample_prefix(w.text, CPU_SAMPLE_PAIRS)
+    sample = sample_prefix(w.text, REF_STEP_PAIRS)
     vals = []
     for i in range(args.warmup + args.steps):
-        cb, r = cpu_baseline(sample, w.k, CPU_SAMPLE_PAIRS)
+        cb, r = cpu_baseline(sample, w.k, REF_STEP_PAIRS)
         if i >= args.warmup:
             vals.append(cb["value"])
     v = statistics.median(vals)

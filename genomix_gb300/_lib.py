@@ -21,7 +21,7 @@ INPUT_READID, INPUT_FASTQ = 0, 1
 EXPORTS = [
     "gx_status_str", "gx_ctx_create", "gx_ctx_destroy", "gx_ctx_mark", "gx_ctx_elapsed_ms", "gx_ctx_synchronize",
     "gx_job_create", "gx_job_add_input", "gx_job_add_input_device", "gx_job_run", "gx_job_emit",
-    "gx_job_records_device", "gx_job_stats", "gx_job_destroy", "gx_batch_run", "gx_pinned_alloc",
+    "gx_job_emit_rewind", "gx_job_records_device", "gx_job_stats", "gx_job_destroy", "gx_batch_run", "gx_pinned_alloc",
     "gx_pinned_free", "gx_fastq_to_readid", "gx_host_free", "gx_seqfile_write", "gx_seqfile_read",
     "gx_records_to_text",
 ]
@@ -85,6 +85,7 @@ def load():
         "gx_job_add_input_device": ([vp, vp, sz, i], i),
         "gx_job_run": ([vp], i),
         "gx_job_emit": ([vp, i, vp, sz, P(sz), P(i)], i),
+        "gx_job_emit_rewind": ([vp, i], i),
         "gx_job_records_device": ([vp, P(vp), P(sz), P(P(ctypes.c_uint64))], i),
         "gx_job_stats": ([vp, P(Stats)], i),
         "gx_job_destroy": ([vp], None),

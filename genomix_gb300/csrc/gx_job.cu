@@ -394,6 +394,15 @@ gx_status gx_job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *w
     return GX_OK;
 }
 
+gx_status gx_job_emit_rewind(gx_job *j, int part) {
+    if (!j) return GX_EINVAL;
+    if (j->state != JS_RAN) return GX_ESTATE;
+    if (part < -1 || part >= j->o.out_parts) return GX_EINVAL;
+    for (int q = 0; q < j->o.out_parts; q++)
+        if (part == -1 || part == q) j->cursor[q] = j->part_bounds[q];
+    return GX_OK;
+}
+
 void gx_job_destroy(gx_job *j) {
     if (!j) return;
     {
@@ -626,6 +635,7 @@ static gx_status run_job(gx_job *j) {
                 CK(cudaMemcpy(&v, part_off + tp, 8, cudaMemcpyDeviceToHost));
             j->part_bounds[q] = v;
         }
+        for (int q = 0; q < P; q++) j->cursor[q] = j->part_bounds[q];
         // node and read-head totals
         {
             std::vector<uint32_t> pn(nparts), hc(nparts);

@@ -473,15 +473,18 @@ __global__ void __launch_bounds__(256) k_insert(typename SlotOf<K>::T *table, ui
         const uint32_t nk = L - (uint32_t)k + 1;
         uint32_t d = fwd <= rc ? 0u : 1u;  // 0 = FORWARD
         uint32_t pd = 0;
+        uint64_t h = KeyOps<K>::hash(d == 0 ? fwd : rc);
         for (uint32_t j = 0; j < nk; j++) {
             const bool hn = j + 1 < nk;
             K nf = fwd, nr = rc;
             uint32_t nd = 0, x = 0;
+            uint64_t hnext = 0;
             if (hn) {
                 x = base_code(s[j + k]);
                 nf = (fwd >> 2) | ((K)x << sh);
                 nr = ((rc << 2) | (K)(3u - x)) & mask;
                 nd = nf <= nr ? 0u : 1u;
+                hnext = KeyOps<K>::hash(nd == 0 ? nf : nr);
             }
             uint32_t bits = 0;
             if (hn) bits |= 1u << (4 * (2 * d + nd) + (d == 0 ? x : 3u - x));
@@ -491,7 +494,6 @@ __global__ void __launch_bounds__(256) k_insert(typename SlotOf<K>::T *table, ui
             }
             if (j == 0) bits |= d == 0 ? META_UNFLIPPED : META_FLIPPED;
             const K canon = d == 0 ? fwd : rc;
-            const uint64_t h = KeyOps<K>::hash(canon);
             const uint32_t p = hash_partition(h, nparts);
             uint32_t probes;
             const int si = table_insert(table + (size_t)p * PART_SLOTS, PART_SLOTS - 1, canon, (uint32_t)h, bits,
@@ -511,6 +513,7 @@ __global__ void __launch_bounds__(256) k_insert(typename SlotOf<K>::T *table, ui
             d = nd;
             fwd = nf;
             rc = nr;
+            h = hnext;
         }
     }
     maxp = __reduce_max_sync(0xffffffffu, maxp);
@@ -642,6 +645,30 @@ template <> struct EmitSmem<u128> {
     }
 };
 
+template <class K> struct SlotLoad;
+template <> struct SlotLoad<uint64_t> {
+    // whole slot in one 16-byte load
+    __device__ __forceinline__ static void get(const Slot64 *s, uint64_t &key, uint32_t &cnt, uint32_t &meta,
+                                               bool &occ) {
+        const ulonglong2 v = ld_cg16(s);
+        occ = v.x != 0;
+        key = v.x - 1;
+        cnt = (uint32_t)v.y;
+        meta = (uint32_t)(v.y >> 32);
+    }
+};
+template <> struct SlotLoad<u128> {
+    __device__ __forceinline__ static void get(const Slot128 *s, u128 &key, uint32_t &cnt, uint32_t &meta,
+                                               bool &occ) {
+        const ulonglong2 a = ld_cg16(&s->lo1), b = ld_cg16(&s->count);
+        const u128 k1 = ((u128)a.y << 64) | a.x;
+        occ = k1 != 0;
+        key = k1 - 1;
+        cnt = (uint32_t)b.x;
+        meta = (uint32_t)(b.x >> 32);
+    }
+};
+
 template <class K>
 struct PrepSmem {
     K key[PART_SLOTS];
@@ -674,16 +701,22 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_prepare(EmitArgs a) {
     const int nb = (a.k + 3) / 4;
     if (threadIdx.x == 0) sm.n = 0;
     __syncthreads();
-    // 1. compact occupied slots
-    for (uint32_t i = threadIdx.x; i < PART_SLOTS; i += blockDim.x) {
-        bool occ;
-        const K key = EmitSmem<K>::load_key1(part + i, occ);
-        if (occ) {
+    // 1. compact occupied slots (all of a thread's slots are loaded before any is used)
+    {
+        constexpr int PER = PART_SLOTS / EMIT_THREADS;
+        K kk[PER];
+        uint32_t cc[PER], mm[PER];
+        bool oo[PER];
+#pragma unroll
+        for (int q = 0; q < PER; q++) SlotLoad<K>::get(part + threadIdx.x + q * EMIT_THREADS, kk[q], cc[q], mm[q], oo[q]);
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            if (!oo[q]) continue;
             const uint32_t j = atomicAdd(&sm.n, 1u);
-            sm.key[j] = key;
-            sm.cnt[j] = part[i].count;
-            sm.meta[j] = part[i].meta;
-            sm.slot[j] = (uint16_t)i;
+            sm.key[j] = kk[q];
+            sm.cnt[j] = cc[q];
+            sm.meta[j] = mm[q];
+            sm.slot[j] = (uint16_t)(threadIdx.x + q * EMIT_THREADS);
             sm.ord[j] = (uint16_t)j;
         }
     }
@@ -774,8 +807,9 @@ void launch_emit_prepare(const EmitArgs &a, cudaStream_t s) {
 struct Sink {
     uint8_t *st;
     long long lo, hi;
+    bool all_in;  // the whole record lies inside the window: no per-byte check
     __device__ __forceinline__ void b(long long pos, uint32_t v) const {
-        if (pos >= lo && pos < hi) st[pos - lo] = (uint8_t)v;
+        if (all_in || (pos >= lo && pos < hi)) st[pos - lo] = (uint8_t)v;
     }
     __device__ __forceinline__ void u32(long long pos, uint32_t v) const {
         b(pos, v >> 24);
@@ -783,7 +817,9 @@ struct Sink {
         b(pos + 2, v >> 8);
         b(pos + 3, v);
     }
-    __device__ __forceinline__ bool touches(long long pos, long long n) const { return pos < hi && pos + n > lo; }
+    __device__ __forceinline__ bool touches(long long pos, long long n) const {
+        return all_in || (pos < hi && pos + n > lo);
+    }
 };
 
 // VKmer bytes of a k-mer value: int32 BE k, then nb bytes of V big-endian (VKmer.write)
@@ -813,13 +849,35 @@ __device__ __forceinline__ long long put_seq(const Sink &o, long long pos, const
     return pos + nbr;
 }
 
+// packs L letters of s (4 per byte, as put_seq) with one warp: lane l writes bytes l, l+32, ...
+__device__ __forceinline__ void pack_seq_warp(const Sink &o, long long pos, const uint8_t *s, uint32_t L, int lane) {
+    const uint32_t nbr = packed_len(L);
+    for (uint32_t j = lane; j < nbr; j += 32) {
+        if (!o.touches(pos + j, 1)) continue;
+        const uint32_t i0 = 4 * (nbr - 1 - j);
+        uint32_t c[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) c[q] = i0 + q < L ? (uint32_t)s[i0 + q] : (uint32_t)'A';
+        uint32_t v = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) v |= base_code_checked(c[q]) << (2 * q);
+        o.b(pos + j, v);
+    }
+}
+
 template <class K>
 struct WriteSmem {
     K key[PART_SLOTS];
     uint32_t cnt[PART_SLOTS];
     uint32_t meta[PART_SLOTS];
     uint32_t off[PART_SLOTS];
+    // read heads of the partition (when at most HEAD_CAP): node rank | flipped << 15, read
+    // ordinal, sequence lengths and the partition-local position of the head's bytes
     uint16_t hrank[HEAD_CAP];
+    uint32_t hread[HEAD_CAP];
+    uint32_t hL[HEAD_CAP];
+    uint32_t hLm[HEAD_CAP];
+    uint32_t hpos[HEAD_CAP];
     __align__(16) uint8_t stage[EMIT_STAGE_BYTES + 32];
     unsigned long long ws[33];
 };
@@ -837,16 +895,62 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_write(EmitArgs a) {
     const unsigned long long base = a.part_off[p];
     const uint32_t hb = a.head_off[p], hc = a.head_cnt2[p];
     const bool hsm = hc <= HEAD_CAP;
-    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-        bool occ;
-        sm.key[j] = EmitSmem<K>::load_key1(part + j, occ);
-        sm.cnt[j] = part[j].count;
-        sm.meta[j] = part[j].meta;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    // nodes: up to PART_SLOTS / EMIT_THREADS independent loads per thread
+    constexpr int PER = PART_SLOTS / EMIT_THREADS;
+    {
+        K kk[PER];
+        uint32_t cc[PER], mm[PER];
+        bool oo[PER];
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            const uint32_t j = threadIdx.x + q * EMIT_THREADS;
+            oo[q] = false;
+            if (j < n) SlotLoad<K>::get(part + j, kk[q], cc[q], mm[q], oo[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            const uint32_t j = threadIdx.x + q * EMIT_THREADS;
+            if (j < n) {
+                sm.key[j] = kk[q];
+                sm.cnt[j] = cc[q];
+                sm.meta[j] = mm[q];
+            }
+        }
     }
-    if (hsm)
-        for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) sm.hrank[i] = (uint16_t)a.heads[a.head_idx[hb + i]].slot;
+    if (hsm) {
+        for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
+            const uint32_t r = a.head_idx[hb + i];
+            const Head h = a.heads[r];
+            const uint32_t rl = a.reads[r];
+            const LineRec lr = a.lines[rl >> 1];
+            const uint32_t mate = rl & 1u;
+            sm.hread[i] = r;
+            sm.hrank[i] = (uint16_t)(h.slot | ((h.uuid >> 40) != 0 ? 0x8000u : 0u));
+            sm.hL[i] = mate ? lr.l1 : lr.l0;
+            sm.hLm[i] = mate ? lr.l0 : lr.l1;
+        }
+    }
     __syncthreads();
-    auto hrank = [&](uint32_t i) -> uint32_t { return hsm ? sm.hrank[i] : a.heads[a.head_idx[hb + i]].slot; };
+    auto hrank = [&](uint32_t i) -> uint32_t {
+        return hsm ? (uint32_t)(sm.hrank[i] & 0x7fffu) : a.heads[a.head_idx[hb + i]].slot;
+    };
+    auto hflip = [&](uint32_t i) -> uint32_t {
+        return hsm ? (uint32_t)(sm.hrank[i] >> 15) : ((a.heads[a.head_idx[hb + i]].uuid >> 40) != 0 ? 1u : 0u);
+    };
+    auto hsize = [&](uint32_t i) -> uint32_t {
+        uint32_t L, Lm;
+        if (hsm) {
+            L = sm.hL[i];
+            Lm = sm.hLm[i];
+        } else {
+            const uint32_t rl = a.reads[a.head_idx[hb + i]];
+            const LineRec lr = a.lines[rl >> 1];
+            L = (rl & 1u) ? lr.l1 : lr.l0;
+            Lm = (rl & 1u) ? lr.l0 : lr.l1;
+        }
+        return 1 + 8 + 4 + packed_len(L) + (Lm > 0 ? 4 + packed_len(Lm) : 0);
+    };
     // first head index of node j (heads are sorted by node rank)
     auto head_lb = [&](uint32_t j) -> uint32_t {
         uint32_t lo = 0, hi = hc;
@@ -859,19 +963,23 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_write(EmitArgs a) {
         }
         return lo;
     };
+    auto edge_bytes = [&](uint32_t meta) -> uint32_t {
+        uint32_t b = 0;
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const uint32_t m = (meta >> (4 * t)) & 15u;
+            if (m) b += 4 + __popc(m) * (4 + nb);
+        }
+        return b;
+    };
     // record sizes and offsets: thread t owns a contiguous node range
     const uint32_t npt = (n + blockDim.x - 1) / blockDim.x;
     const uint32_t j0 = min(n, threadIdx.x * npt), j1 = min(n, j0 + npt);
     unsigned long long mine = 0;
     for (uint32_t j = j0; j < j1; j++) {
         uint32_t sz = node_base_bytes(sm.meta[j], nb);
-        if (sm.meta[j] & (META_UNFLIPPED | META_FLIPPED)) {
-            for (uint32_t h = head_lb(j); h < hc && hrank(h) == j; h++) {
-                const uint32_t r = a.head_idx[hb + h];
-                const uint32_t rl = a.reads[r];
-                sz += head_bytes(a.lines[rl >> 1], rl & 1u);
-            }
-        }
+        if (sm.meta[j] & (META_UNFLIPPED | META_FLIPPED))
+            for (uint32_t h = head_lb(j); h < hc && hrank(h) == j; h++) sz += hsize(h);
         sm.off[j] = sz;  // size for now
         mine += sz;
     }
@@ -880,6 +988,20 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_write(EmitArgs a) {
     for (uint32_t j = j0; j < j1; j++) {
         const uint32_t sz = sm.off[j];
         sm.off[j] = (uint32_t)run;
+        if (hsm && (sm.meta[j] & (META_UNFLIPPED | META_FLIPPED))) {
+            // positions of the node's read heads: after frame, key, active byte and edges
+            long long pos = (long long)run + 8 + (4 + nb) + 1 + edge_bytes(sm.meta[j]);
+            const uint32_t h0 = head_lb(j);
+            for (uint32_t fl = 0; fl < 2; fl++) {
+                if (!(sm.meta[j] & (fl == 0 ? META_UNFLIPPED : META_FLIPPED))) continue;
+                pos += 5;
+                for (uint32_t h = h0; h < hc && hrank(h) == j; h++) {
+                    if (hflip(h) != fl) continue;
+                    sm.hpos[h] = (uint32_t)pos;
+                    pos += hsize(h);
+                }
+            }
+        }
         run += sz;
     }
     if (threadIdx.x == 0 && tot != pbytes) atomicAdd(&a.st->internal_err, 1u);
@@ -888,12 +1010,14 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_write(EmitArgs a) {
     const long long my_hi = j0 < j1 ? (long long)(j1 == n ? tot : sm.off[j1]) : 0;
     for (unsigned long long W = 0; W < tot; W += EMIT_STAGE_BYTES) {
         const unsigned long long wlen = min((unsigned long long)EMIT_STAGE_BYTES, tot - W);
-        const Sink o{sm.stage, (long long)W, (long long)(W + wlen)};
-        if (j0 < j1 && my_lo < o.hi && my_hi > o.lo) {
+        const Sink ow{sm.stage, (long long)W, (long long)(W + wlen), false};
+        if (j0 < j1 && my_lo < ow.hi && my_hi > ow.lo) {
             for (uint32_t j = j0; j < j1; j++) {
                 const long long st = sm.off[j];
                 const long long en = j + 1 < n ? (long long)sm.off[j + 1] : (long long)tot;
-                if (!o.touches(st, en - st)) continue;
+                if (!ow.touches(st, en - st)) continue;
+                Sink o = ow;
+                o.all_in = st >= ow.lo && en <= ow.hi;
                 const K key = sm.key[j];
                 const uint32_t meta = sm.meta[j];
                 const uint32_t key_len = 4 + nb;
@@ -933,43 +1057,57 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_write(EmitArgs a) {
                     uint32_t h1 = h0;
                     while (h1 < hc && hrank(h1) == j) h1++;
                     // unflipped set, then flipped set (uuid offset 0 sorts first)
-                    for (int fl = 0; fl < 2; fl++) {
+                    for (uint32_t fl = 0; fl < 2; fl++) {
                         const uint32_t flag = fl == 0 ? META_UNFLIPPED : META_FLIPPED;
                         if (!(meta & flag)) continue;
                         uint32_t cnt = 0;
-                        for (uint32_t h = h0; h < h1; h++) {
-                            const bool f = (a.heads[a.head_idx[hb + h]].uuid >> 40) != 0;
-                            if ((int)f == fl) cnt++;
-                        }
+                        for (uint32_t h = h0; h < h1; h++) cnt += hflip(h) == fl ? 1u : 0u;
                         o.b(pos++, 1);  // ExternalableTreeSet: whole body in stream
                         o.u32(pos, cnt);
                         pos += 4;
                         for (uint32_t h = h0; h < h1; h++) {
-                            const uint32_t r = a.head_idx[hb + h];
-                            const Head hd = a.heads[r];
-                            if ((int)((hd.uuid >> 40) != 0) != fl) continue;
-                            const uint32_t rl = a.reads[r];
-                            const LineRec lr = a.lines[rl >> 1];
-                            const uint32_t mate = rl & 1u;
-                            const uint32_t hsz = head_bytes(lr, mate);
+                            if (hflip(h) != fl) continue;
+                            const uint32_t hsz = hsize(h);
                             if (!o.touches(pos, hsz)) {
                                 pos += hsz;
                                 continue;
                             }
+                            const uint32_t r = a.head_idx[hb + h];
+                            const unsigned long long uuid = a.heads[r].uuid;
+                            const uint32_t rl = a.reads[r];
+                            const LineRec lr = a.lines[rl >> 1];
+                            const uint32_t mate = rl & 1u;
                             const uint32_t L = mate ? lr.l1 : lr.l0, Lm = mate ? lr.l0 : lr.l1;
-                            const uint8_t *sq = a.text + (mate ? lr.s1 : lr.s0);
-                            const uint8_t *sm_ = a.text + (mate ? lr.s0 : lr.s1);
-                            o.b(pos++, Lm > 0 ? 1u : 0u);
-                            o.u32(pos, (uint32_t)(hd.uuid >> 32));
-                            o.u32(pos + 4, (uint32_t)hd.uuid);
-                            pos += 8;
-                            pos = put_seq(o, pos, sq, L);
-                            if (Lm > 0) pos = put_seq(o, pos, sm_, Lm);
+                            o.b(pos, Lm > 0 ? 1u : 0u);
+                            o.u32(pos + 1, (uint32_t)(uuid >> 32));
+                            o.u32(pos + 5, (uint32_t)uuid);
+                            o.u32(pos + 9, L);
+                            if (Lm > 0) o.u32(pos + 13 + packed_len(L), Lm);
+                            if (!hsm) {  // large head sets: this thread packs the letters too
+                                put_seq(o, pos + 9, a.text + (mate ? lr.s1 : lr.s0), L);
+                                if (Lm > 0) put_seq(o, pos + 13 + packed_len(L), a.text + (mate ? lr.s0 : lr.s1), Lm);
+                            }
+                            pos += hsz;
                         }
                     }
                 }
                 const float cov = (float)sm.cnt[j];
                 o.u32(pos, __float_as_uint(cov));
+            }
+        }
+        if (hsm) {
+            const Sink o = ow;
+            // read and mate letters of the partition's heads: one warp per head
+            for (uint32_t h = warp; h < hc; h += nwarp) {
+                const uint32_t L = sm.hL[h], Lm = sm.hLm[h];
+                const long long hp = sm.hpos[h];
+                const uint32_t hsz = 13 + packed_len(L) + (Lm > 0 ? 4 + packed_len(Lm) : 0);
+                if (!o.touches(hp, hsz)) continue;
+                const uint32_t rl = a.reads[sm.hread[h]];
+                const LineRec lr = a.lines[rl >> 1];
+                const uint32_t mate = rl & 1u;
+                pack_seq_warp(o, hp + 13, a.text + (mate ? lr.s1 : lr.s0), L, lane);
+                if (Lm > 0) pack_seq_warp(o, hp + 17 + packed_len(L), a.text + (mate ? lr.s0 : lr.s1), Lm, lane);
             }
         }
         __syncthreads();

@@ -18,7 +18,7 @@ constexpr int PART_SLOTS_LOG2 = 11;  // slots per table partition (both key widt
 constexpr uint32_t PART_SLOTS = 1u << PART_SLOTS_LOG2;
 constexpr int EMIT_THREADS = 256;
 constexpr uint32_t HEAD_CAP = 1024;         // read heads per partition sorted in shared memory
-constexpr uint32_t EMIT_STAGE_BYTES = 24576;  // output staging window per partition CTA
+constexpr uint32_t EMIT_STAGE_BYTES = 16384;  // output staging window per partition CTA
 
 // Kernel launches made by the calling host thread (read before and after a run).
 uint64_t launches_this_thread();

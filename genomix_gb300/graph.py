@@ -191,6 +191,7 @@ class GraphBuildJob:
         """Serialized record stream of one part (or all parts in order) as bytes."""
         parts = range(self.out_parts) if part is None else [part]
         offs = self.part_offsets()
+        _check(self._L.gx_job_emit_rewind(self.h, -1 if part is None else part), "gx_job_emit_rewind")
         out = []
         for q in parts:
             total = offs[q + 1] - offs[q]

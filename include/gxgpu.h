@@ -155,6 +155,9 @@ gx_status gx_job_run(gx_job *job);
  * stopped; *more is 1 while bytes remain.  Each call ends on a record boundary. */
 gx_status gx_job_emit(gx_job *job, int part, void *host_out, size_t cap, size_t *written, int *more);
 
+/* Restart gx_job_emit of output part `part` (-1: every part) from its first record. */
+gx_status gx_job_emit_rewind(gx_job *job, int part);
+
 /* Device view of the whole record stream (all parts in order) and the per-part byte
  * offsets (out_parts + 1 entries, host memory, owned by the job). */
 gx_status gx_job_records_device(gx_job *job, const void **dev, size_t *bytes,
