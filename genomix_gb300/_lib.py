@@ -16,6 +16,7 @@ STATUS_NAMES = {
     10: "GX_ESTATE", 11: "GX_ECANCELLED", 12: "GX_EFASTQ_PAIRING", 13: "GX_EBUSY", 14: "GX_EAGAIN",
 }
 INPUT_READID, INPUT_FASTQ = 0, 1
+ALGO_DEFAULT, ALGO_PARTITIONED, ALGO_TABLE = 0, 1, 2
 
 # every symbol include/gxgpu.h declares
 EXPORTS = [
@@ -42,6 +43,7 @@ class JobOpts(ctypes.Structure):
         ("max_readids_per_edge", ctypes.c_int),
         ("threads_per_read", ctypes.c_int),
         ("est_input_bytes", ctypes.c_size_t),
+        ("algorithm", ctypes.c_int),
     ]
 
 

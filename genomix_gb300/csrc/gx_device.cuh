@@ -159,6 +159,21 @@ __device__ __forceinline__ void cas128(unsigned long long *p, unsigned long long
         : "memory");
 }
 
+__device__ __forceinline__ void cas128_shared(void *p, unsigned long long clo, unsigned long long chi,
+                                              unsigned long long vlo, unsigned long long vhi, unsigned long long &olo,
+                                              unsigned long long &ohi) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile(
+        "{\n\t.reg .b128 d, b, c;\n\t"
+        "mov.b128 b, {%2, %3};\n\t"
+        "mov.b128 c, {%4, %5};\n\t"
+        "atom.shared.cas.b128 d, [%6], b, c;\n\t"
+        "mov.b128 {%0, %1}, d;\n\t}"
+        : "=l"(olo), "=l"(ohi)
+        : "l"(clo), "l"(chi), "l"(vlo), "l"(vhi), "r"(a)
+        : "memory");
+}
+
 // Insert one occurrence: count += 1, meta |= bits.  Linear probing inside the key's
 // partition, at most `smask + 1` probes.  Returns the slot index or -1 (partition full).
 __device__ __forceinline__ int table_insert(Slot64 *part, uint32_t smask, uint64_t key, uint32_t h, uint32_t bits,
@@ -198,7 +213,9 @@ __device__ __forceinline__ int table_insert(Slot128 *part, uint32_t smask, u128 
         ulonglong2 cm = ld_cg16(&s->count);
         unsigned long long clo = kv.x, chi = kv.y;
         uint32_t meta = (uint32_t)(cm.x >> 32);
-        if (clo == 0ULL && chi == 0ULL) {
+        if (clo != wlo || chi != whi) {
+            // a 16-byte load is not guaranteed to be single-copy atomic: decide claim / hit /
+            // occupied from the value the CAS returns, which is
             cas128(&s->lo1, 0ULL, 0ULL, wlo, whi, clo, chi);
             if (clo == 0ULL && chi == 0ULL) {
                 clo = wlo;
@@ -234,6 +251,18 @@ struct Head {
     uint32_t part;  // table partition of the first k-mer
     uint32_t slot;  // slot in the partition; after compaction, the node's rank
     unsigned long long uuid;
+    unsigned long long klo, khi;  // canonical first k-mer (the partitioned build looks it up)
+};
+
+// A read head as the record writer needs it, in the partition's output order (partitioned
+// build): the head's byte position in its partition's records and, on the first head of a
+// set, the set's size.
+struct HeadOut {
+    unsigned long long uuid;
+    unsigned long long s_off, m_off;  // text offsets of the read and of its mate
+    uint32_t pos;                     // partition-local byte position of the ReadHeadInfo
+    uint32_t set_count;               // > 0 on the first head of a set: heads in the set
+    uint32_t L, Lm;                   // read and mate lengths (Lm = 0: no mate sequence)
 };
 
 // ---- per-line parse output ---------------------------------------------------------------

@@ -248,7 +248,6 @@ gx_status gx_job_create(gx_ctx *c, const gx_job_opts *opts, gx_job **out) {
     j->ctx = c;
     j->o = *opts;
     if (j->o.out_parts == 0) j->o.out_parts = 1;
-    if (j->o.load_factor == 0) j->o.load_factor = 0.5;
     j->k = opts->kmer_length;
     j->wide = j->k > 32 ? 1 : 0;
     cudaSetDevice(c->device);
@@ -434,12 +433,367 @@ gx_status gx_batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses) {
 // ---------------------------------------------------------------------------------------
 // the run
 // ---------------------------------------------------------------------------------------
+// state shared by the phases of one run
+struct RunCtx {
+    gx_job *j;
+    cudaStream_t s;
+    RunArena &ar;
+    DevStatus *d_st;
+    void *scratch;
+    const uint8_t *text;
+    uint64_t n_text;
+    LineRec *lines;
+    uint32_t *reads;
+    uint32_t n_lines, n_reads;
+    unsigned long long n_occ;
+    // partitioned build: A1 results (2048 super counts, HyperLogLog registers)
+    uint32_t *d_scnt, *d_hll;
+    std::vector<uint32_t> scnt, hll;
+};
+
+static gx_status finish_outputs(RunCtx &rc, uint32_t nparts, unsigned long long total, unsigned long long *part_off,
+                                const uint32_t *part_nodes, const uint32_t *head_cnt2, void *outp) {
+    gx_job *j = rc.j;
+    const int P = j->o.out_parts;
+    for (int q = 0; q <= P; q++) {
+        const uint64_t tp = (uint64_t)nparts * q / P;
+        unsigned long long v = 0;
+        if (q == P)
+            v = total;
+        else if (tp > 0)
+            CK(cudaMemcpy(&v, part_off + tp, 8, cudaMemcpyDeviceToHost));
+        j->part_bounds[q] = v;
+    }
+    for (int q = 0; q < P; q++) j->cursor[q] = j->part_bounds[q];
+    std::vector<uint32_t> pn(nparts), hc(nparts);
+    CK(cudaMemcpy(pn.data(), part_nodes, nparts * 4ull, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hc.data(), head_cnt2, nparts * 4ull, cudaMemcpyDeviceToHost));
+    uint64_t nn = 0, nh = 0;
+    for (uint32_t q = 0; q < nparts; q++) {
+        nn += pn[q];
+        nh += hc[q];
+    }
+    j->st.nodes = nn;
+    j->st.read_heads = nh;
+    j->d_out = (uint8_t *)outp;
+    j->out_bytes = total;
+    j->d_part_off = part_off;
+    j->nparts = nparts;
+    j->st.record_bytes = total;
+    return GX_OK;
+}
+
+// ---- the global-table build ------------------------------------------------------------
+static gx_status build_table(RunCtx &rc) {
+    gx_job *j = rc.j;
+    cudaStream_t s = rc.s;
+    Timers &tm = j->tm;
+    gx_status e;
+    const int k = j->k;
+    const uint32_t n_reads = rc.n_reads;
+    const size_t slot_bytes = j->wide ? sizeof(Slot128) : sizeof(Slot64);
+    double lf = j->o.load_factor > 0 ? j->o.load_factor : 0.5;
+    DevStatus hs;
+    for (int attempt = 0;; attempt++) {
+        const uint64_t want = (uint64_t)((double)rc.n_occ / lf) + 1;
+        const uint64_t nparts64 = std::max<uint64_t>(1, (want + PART_SLOTS - 1) / PART_SLOTS);
+        if (nparts64 > 0x7fffffffULL) return GX_ENOMEM;
+        const uint32_t nparts = (uint32_t)nparts64;
+        const size_t table_bytes = (size_t)nparts * PART_SLOTS * slot_bytes;
+        if (table_bytes > j->ctx->mem_limit) return GX_ENOMEM;
+        RunArena tar(s);
+        void *table;
+        Head *heads;
+        uint32_t *head_cnt, *head_off, *head_cur, *head_idx, *head_cnt2, *part_nodes;
+        unsigned long long *head_sk, *part_bytes, *part_off;
+        if ((e = tar.alloc(table, table_bytes / 16 * 16 + 16)) != GX_OK) return e;
+        if ((e = tar.alloc(heads, n_reads)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cnt, nparts)) != GX_OK) return e;
+        if ((e = tar.alloc(head_off, nparts)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cur, nparts)) != GX_OK) return e;
+        if ((e = tar.alloc(head_idx, n_reads)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cnt2, nparts)) != GX_OK) return e;
+        if ((e = tar.alloc(head_sk, n_reads)) != GX_OK) return e;
+        if ((e = tar.alloc(part_nodes, nparts)) != GX_OK) return e;
+        if ((e = tar.alloc(part_bytes, nparts)) != GX_OK) return e;
+        void *pscratch;
+        if ((e = tar.alloc(pscratch, scan_scratch_bytes(nparts, 8))) != GX_OK) return e;
+        void *part_off_v = nullptr;
+        CK(cudaMallocAsync(&part_off_v, (nparts + 1) * sizeof(unsigned long long), s));
+        part_off = (unsigned long long *)part_off_v;
+
+        TableGeom g{table, nparts, j->wide};
+        CK(cudaMemsetAsync(table, 0, table_bytes, s));
+        CK(cudaMemsetAsync(head_cnt, 0, nparts * 4ull, s));
+        CK(cudaMemsetAsync(head_cur, 0, nparts * 4ull, s));
+        CK(cudaEventRecord(tm.ev[2], s));
+        launch_insert(g, rc.text, rc.lines, rc.reads, n_reads, k, heads, head_cnt, rc.d_st, s);
+        CK(cudaEventRecord(tm.ev[3], s));
+        exclusive_scan_u32(head_cnt, head_off, nparts, nullptr, pscratch, s);
+        launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, nparts, s);
+        EmitArgs a{};
+        a.g = g;
+        a.k = k;
+        a.text = rc.text;
+        a.lines = rc.lines;
+        a.reads = rc.reads;
+        a.heads = heads;
+        a.head_idx = head_idx;
+        a.head_sk = head_sk;
+        a.head_off = head_off;
+        a.head_cnt = head_cnt;
+        a.head_cnt2 = head_cnt2;
+        a.part_nodes = part_nodes;
+        a.part_bytes = part_bytes;
+        a.part_off = part_off;
+        a.st = rc.d_st;
+        launch_emit_prepare(a, s);
+        exclusive_scan_u64(part_bytes, part_off, nparts, part_off + nparts, pscratch, s);
+        CK(cudaEventRecord(tm.ev[4], s));
+        unsigned long long total = 0;
+        CK(cudaMemcpyAsync(&hs, rc.d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&total, part_off + nparts, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaGetLastError());
+        if (hs.table_full) {
+            cudaFreeAsync(part_off, s);
+            DevStatus zero{};
+            zero.parse_err = ~0ULL;
+            CK(cudaMemcpyAsync(rc.d_st, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
+            if (attempt >= 2) return GX_ETABLE_FULL;
+            lf *= 0.5;
+            continue;
+        }
+        void *outp = nullptr;
+        CK(cudaMallocAsync(&outp, total + 16, s));
+        if (((uintptr_t)outp & 15) != 0) {  // the record writer stores aligned 16-byte vectors
+            cudaFreeAsync(outp, s);
+            cudaFreeAsync(part_off, s);
+            return GX_ECUDA;
+        }
+        a.out = (uint8_t *)outp;
+        CK(cudaEventRecord(tm.ev[5], s));
+        launch_emit_write(a, s);
+        CK(cudaEventRecord(tm.ev[6], s));
+        CK(cudaMemcpyAsync(&hs, rc.d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaGetLastError());
+        if (hs.internal_err) {
+            cudaFreeAsync(outp, s);
+            cudaFreeAsync(part_off, s);
+            fprintf(stderr, "gxgpu: internal error: record sizes disagree between emission passes\n");
+            return GX_ECUDA;
+        }
+        if ((e = finish_outputs(rc, nparts, total, part_off, part_nodes, head_cnt2, outp)) != GX_OK) return e;
+        j->st.table_slots = (uint64_t)nparts * PART_SLOTS;
+        j->st.table_partitions = nparts;
+        j->st.max_probe = hs.max_probe;
+        j->st.cov_inexact_nodes = hs.cov_inexact;
+        j->st.ms_insert = tm.ms(2, 3);
+        j->st.ms_emit = tm.ms(3, 4) + tm.ms(5, 6);
+        j->st.ms_total = tm.ms(0, 6);
+        return GX_OK;
+    }
+}
+
+// ---- the partitioned build --------------------------------------------------------------
+static gx_status build_partitioned(RunCtx &rc) {
+    gx_job *j = rc.j;
+    cudaStream_t s = rc.s;
+    Timers &tm = j->tm;
+    gx_status e;
+    const int k = j->k, wide = j->wide;
+    const uint32_t n_reads = rc.n_reads;
+    const uint64_t n_occ = rc.n_occ;
+    const size_t kb = wide ? 16 : 8;
+    const double d_est = hll_estimate(rc.hll.data());
+    double safety = 1.15;
+    DevStatus hs;
+    for (int attempt = 0;; attempt++) {
+        const double target = j->o.load_factor > 0 ? j->o.load_factor * AGG_SLOTS : (double)AGG_TARGET;
+        const PartPlan pp = plan_partitions(d_est, safety, target);
+        const uint32_t S = 1u << pp.log_s, P = pp.P;
+        // super counts at this resolution, offsets and CHUNK-sized pieces
+        std::vector<unsigned long long> soff(S + 1, 0);
+        const uint32_t fold = MAX_SUPERS >> pp.log_s;
+        for (uint32_t q = 0; q < S; q++) {
+            unsigned long long c = 0;
+            for (uint32_t t = 0; t < fold; t++) c += rc.scnt[q * fold + t];
+            soff[q + 1] = soff[q] + c;
+        }
+        if (soff[S] != n_occ) return GX_ECUDA;
+        std::vector<ulonglong2> chunks;
+        chunks.reserve(n_occ / CHUNK + S + 1);
+        for (uint32_t q = 0; q < S; q++)
+            for (unsigned long long st = soff[q]; st < soff[q + 1]; st += CHUNK) {
+                const unsigned long long len = std::min<unsigned long long>(CHUNK, soff[q + 1] - st);
+                chunks.push_back(make_ulonglong2(st, ((unsigned long long)q << 32) | len));
+            }
+        const uint32_t n_chunks = (uint32_t)chunks.size();
+        RunArena tar(s);
+        void *okey, *okey2;
+        uint16_t *obits, *obits2;
+        unsigned long long *d_soff, *fine_cnt, *fine_off, *head_sk, *part_bytes, *part_off;
+        ulonglong2 *d_chunks;
+        uint32_t *s_cur, *fine_cur, *head_cnt, *head_off, *head_cur, *head_idx, *head_cnt2, *part_nodes;
+        Head *heads;
+        HeadOut *hout;
+        uint32_t *noff;
+        uint8_t *okey_b, *okey2_b;
+        if ((e = tar.alloc(okey_b, n_occ * kb)) != GX_OK) return e;
+        if ((e = tar.alloc(okey2_b, n_occ * kb)) != GX_OK) return e;
+        okey = okey_b;
+        okey2 = okey2_b;
+        if ((e = tar.alloc(obits, n_occ)) != GX_OK) return e;
+        if ((e = tar.alloc(obits2, n_occ)) != GX_OK) return e;
+        if ((e = tar.alloc(d_soff, S + 1)) != GX_OK) return e;
+        if ((e = tar.alloc(d_chunks, std::max<uint32_t>(n_chunks, 1))) != GX_OK) return e;
+        if ((e = tar.alloc(s_cur, S)) != GX_OK) return e;
+        if ((e = tar.alloc(fine_cnt, P)) != GX_OK) return e;
+        if ((e = tar.alloc(fine_off, P + 1)) != GX_OK) return e;
+        if ((e = tar.alloc(fine_cur, P)) != GX_OK) return e;
+        if ((e = tar.alloc(heads, n_reads)) != GX_OK) return e;
+        if ((e = tar.alloc(hout, n_reads)) != GX_OK) return e;
+        if ((e = tar.alloc(noff, n_occ)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cnt, P)) != GX_OK) return e;
+        if ((e = tar.alloc(head_off, P)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cur, P)) != GX_OK) return e;
+        if ((e = tar.alloc(head_idx, n_reads)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cnt2, P)) != GX_OK) return e;
+        if ((e = tar.alloc(head_sk, n_reads)) != GX_OK) return e;
+        if ((e = tar.alloc(part_nodes, P)) != GX_OK) return e;
+        if ((e = tar.alloc(part_bytes, P)) != GX_OK) return e;
+        void *pscratch;
+        if ((e = tar.alloc(pscratch, scan_scratch_bytes(P + 1, 8))) != GX_OK) return e;
+        void *part_off_v = nullptr;
+        CK(cudaMallocAsync(&part_off_v, (P + 1) * sizeof(unsigned long long), s));
+        part_off = (unsigned long long *)part_off_v;
+        CK(cudaMemcpyAsync(d_soff, soff.data(), (S + 1) * 8ull, cudaMemcpyHostToDevice, s));
+        if (n_chunks)
+            CK(cudaMemcpyAsync(d_chunks, chunks.data(), n_chunks * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(s_cur, 0, S * 4ull, s));
+        CK(cudaMemsetAsync(fine_cnt, 0, P * 8ull, s));
+        CK(cudaMemsetAsync(fine_cur, 0, P * 4ull, s));
+        CK(cudaMemsetAsync(head_cnt, 0, P * 4ull, s));
+        CK(cudaMemsetAsync(head_cur, 0, P * 4ull, s));
+        CK(cudaEventRecord(tm.ev[2], s));
+        // A2, read heads
+        launch_scatter_super(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, pp.log_s, d_soff, s_cur, okey, obits, s);
+        launch_heads_part(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, pp, heads, head_cnt, s);
+        exclusive_scan_u32(head_cnt, head_off, P, nullptr, pscratch, s);
+        launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, P, s);
+        // B1, B2
+        launch_fine_count(wide, okey, d_chunks, n_chunks, pp, fine_cnt, s);
+        exclusive_scan_u64(fine_cnt, fine_off, P, fine_off + P, pscratch, s);
+        launch_scatter_fine(wide, okey, obits, d_chunks, n_chunks, pp, fine_off, fine_cur, okey2, obits2, s);
+        CK(cudaEventRecord(tm.ev[3], s));
+        // C
+        AggArgs g{};
+        g.wide = wide;
+        g.k = k;
+        g.pp = pp;
+        g.okey2 = okey2;
+        g.obits2 = obits2;
+        g.fine_off = fine_off;
+        g.lines = rc.lines;
+        g.reads = rc.reads;
+        g.heads = heads;
+        g.head_idx = head_idx;
+        g.head_sk = head_sk;
+        g.head_off = head_off;
+        g.head_cnt = head_cnt;
+        g.head_cnt2 = head_cnt2;
+        g.nkey = okey2;
+        g.ncm = (unsigned long long *)okey;
+        g.noff = noff;
+        g.hout = hout;
+        g.part_nodes = part_nodes;
+        g.part_bytes = part_bytes;
+        g.st = rc.d_st;
+        launch_aggregate(g, s);
+        exclusive_scan_u64(part_bytes, part_off, P, part_off + P, pscratch, s);
+        CK(cudaEventRecord(tm.ev[4], s));
+        unsigned long long total = 0;
+        CK(cudaMemcpyAsync(&hs, rc.d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&total, part_off + P, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaGetLastError());
+        if (hs.internal_err) {
+            cudaFreeAsync(part_off, s);
+            fprintf(stderr, "gxgpu: internal error: a read head's k-mer was not aggregated\n");
+            return GX_ECUDA;
+        }
+        if (hs.table_full) {
+            // more distinct k-mers in a bucket than its shared table holds: more buckets
+            cudaFreeAsync(part_off, s);
+            DevStatus zero{};
+            zero.parse_err = ~0ULL;
+            CK(cudaMemcpyAsync(rc.d_st, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
+            if (attempt >= 3 || pp.F >= MAX_FINE) return GX_ETABLE_FULL;
+            safety *= 2;
+            continue;
+        }
+        // D: records
+        void *outp = nullptr;
+        CK(cudaMallocAsync(&outp, total + 16, s));
+        if (((uintptr_t)outp & 15) != 0) {
+            cudaFreeAsync(outp, s);
+            cudaFreeAsync(part_off, s);
+            return GX_ECUDA;
+        }
+        EmitArgs a{};
+        a.g = TableGeom{nullptr, P, wide};
+        a.k = k;
+        a.text = rc.text;
+        a.lines = rc.lines;
+        a.reads = rc.reads;
+        a.heads = heads;
+        a.head_idx = head_idx;
+        a.head_sk = head_sk;
+        a.head_off = head_off;
+        a.head_cnt = head_cnt;
+        a.head_cnt2 = head_cnt2;
+        a.part_nodes = part_nodes;
+        a.part_bytes = part_bytes;
+        a.part_off = part_off;
+        a.out = (uint8_t *)outp;
+        a.st = rc.d_st;
+        a.nkey = okey2;
+        a.ncm = (const unsigned long long *)okey;
+        a.node_base = fine_off;
+        a.noff = noff;
+        a.hout = hout;
+        CK(cudaEventRecord(tm.ev[5], s));
+        launch_emit_write_part(a, s);
+        CK(cudaEventRecord(tm.ev[6], s));
+        CK(cudaMemcpyAsync(&hs, rc.d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaGetLastError());
+        if (hs.internal_err) {
+            cudaFreeAsync(outp, s);
+            cudaFreeAsync(part_off, s);
+            fprintf(stderr, "gxgpu: internal error: record sizes disagree between emission passes\n");
+            return GX_ECUDA;
+        }
+        if ((e = finish_outputs(rc, P, total, part_off, part_nodes, head_cnt2, outp)) != GX_OK) return e;
+        j->st.table_slots = (uint64_t)P * AGG_SLOTS;
+        j->st.table_partitions = P;
+        j->st.max_probe = 0;
+        j->st.cov_inexact_nodes = hs.cov_inexact;
+        j->st.ms_insert = tm.ms(2, 3);
+        j->st.ms_emit = tm.ms(3, 4) + tm.ms(5, 6);
+        j->st.ms_total = tm.ms(0, 6);
+        return GX_OK;
+    }
+}
+
 static gx_status run_job(gx_job *j) {
     cudaStream_t s = j->ctx->stream;
     Timers &tm = j->tm;
     memset(&j->st, 0, sizeof j->st);
     j->st.key_bits = j->wide ? 128 : 64;
     const int k = j->k;
+    const bool partitioned = j->o.algorithm != GX_ALGO_TABLE;
 
     // FASTQ: the reference driver's conversion, then the readid path
     if (j->o.input_kind == GX_INPUT_FASTQ) {
@@ -476,13 +830,19 @@ static gx_status run_job(gx_job *j) {
         CK(cudaMemcpyAsync(d_st, &init, sizeof init, cudaMemcpyHostToDevice, s));
     }
     const uint64_t tiles = line_tiles(n_text);
-    uint32_t *tile_cnt, *d_nlines;
+    uint32_t *tile_cnt, *d_nlines, *d_scnt = nullptr, *d_hll = nullptr;
     void *scratch;
     const size_t scratch_bytes = std::max(scan_scratch_bytes(std::max<uint64_t>(tiles, 1), 8),
                                           scan_scratch_bytes(n_text + 16, 8));
     if ((e = ar.alloc(tile_cnt, tiles + 1)) != GX_OK) return e;
     if ((e = ar.alloc(d_nlines, 4)) != GX_OK) return e;
     if ((e = ar.alloc(scratch, scratch_bytes)) != GX_OK) return e;
+    if (partitioned) {
+        if ((e = ar.alloc(d_scnt, MAX_SUPERS)) != GX_OK) return e;
+        if ((e = ar.alloc(d_hll, HLL_REGS)) != GX_OK) return e;
+        CK(cudaMemsetAsync(d_scnt, 0, MAX_SUPERS * 4, s));
+        CK(cudaMemsetAsync(d_hll, 0, HLL_REGS * 4, s));
+    }
 
     // ---- K1 ----
     CK(cudaEventRecord(tm.ev[0], s));
@@ -505,11 +865,21 @@ static gx_status run_job(gx_job *j) {
     launch_parse_lines(text, n_text, line_end, n_lines, k, lines, lflags, nvalid, d_st, s);
     exclusive_scan_u32(nvalid, nvalid, n_lines, d_nlines + 1, scratch, s);
     launch_read_list(lflags, nvalid, lines, n_lines, k, reads, d_st, s);
+    // A1 of the partitioned build runs before the host learns the read count
+    if (partitioned)
+        launch_count_occ(j->wide, text, n_text, lines, reads, d_nlines + 1, 2 * n_lines, k, 11, d_scnt, d_hll, s);
     CK(cudaEventRecord(tm.ev[1], s));
     DevStatus hs;
     uint32_t n_reads = 0;
+    RunCtx rc{j, s, ar, d_st, scratch, text, n_text, lines, reads, n_lines, 0, 0, d_scnt, d_hll, {}, {}};
     CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(&n_reads, d_nlines + 1, 4, cudaMemcpyDeviceToHost, s));
+    if (partitioned) {
+        rc.scnt.resize(MAX_SUPERS);
+        rc.hll.resize(HLL_REGS);
+        CK(cudaMemcpyAsync(rc.scnt.data(), d_scnt, MAX_SUPERS * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(rc.hll.data(), d_hll, HLL_REGS * 4, cudaMemcpyDeviceToHost, s));
+    }
     CK(cudaStreamSynchronize(s));
     CK(cudaGetLastError());
     if (hs.parse_err != ~0ULL) {
@@ -523,145 +893,7 @@ static gx_status run_job(gx_job *j) {
         j->st.ms_total = tm.ms(0, 1);
         return GX_OK;
     }
-
-    // ---- table ----
-    const size_t slot_bytes = j->wide ? sizeof(Slot128) : sizeof(Slot64);
-    double lf = j->o.load_factor;
-    for (int attempt = 0;; attempt++) {
-        const uint64_t want = (uint64_t)((double)hs.n_occ / lf) + 1;
-        const uint64_t nparts64 = std::max<uint64_t>(1, (want + PART_SLOTS - 1) / PART_SLOTS);
-        if (nparts64 > 0x7fffffffULL) return GX_ENOMEM;
-        const uint32_t nparts = (uint32_t)nparts64;
-        const size_t table_bytes = (size_t)nparts * PART_SLOTS * slot_bytes;
-        if (table_bytes > j->ctx->mem_limit) return GX_ENOMEM;
-        RunArena tar(s);
-        void *table;
-        Head *heads;
-        uint32_t *head_cnt, *head_off, *head_cur, *head_idx, *head_cnt2, *part_nodes;
-        unsigned long long *head_sk, *part_bytes, *part_off;
-        if ((e = tar.alloc(table, table_bytes / 16 * 16 + 16)) != GX_OK) return e;
-        if ((e = tar.alloc(heads, n_reads)) != GX_OK) return e;
-        if ((e = tar.alloc(head_cnt, nparts)) != GX_OK) return e;
-        if ((e = tar.alloc(head_off, nparts)) != GX_OK) return e;
-        if ((e = tar.alloc(head_cur, nparts)) != GX_OK) return e;
-        if ((e = tar.alloc(head_idx, n_reads)) != GX_OK) return e;
-        if ((e = tar.alloc(head_cnt2, nparts)) != GX_OK) return e;
-        if ((e = tar.alloc(head_sk, n_reads)) != GX_OK) return e;
-        if ((e = tar.alloc(part_nodes, nparts)) != GX_OK) return e;
-        if ((e = tar.alloc(part_bytes, nparts)) != GX_OK) return e;
-        void *pscratch;
-        if ((e = tar.alloc(pscratch, scan_scratch_bytes(nparts, 8))) != GX_OK) return e;
-        void *part_off_v = nullptr;
-        CK(cudaMallocAsync(&part_off_v, (nparts + 1) * sizeof(unsigned long long), s));
-        part_off = (unsigned long long *)part_off_v;
-
-        TableGeom g{table, nparts, j->wide};
-        CK(cudaMemsetAsync(table, 0, table_bytes, s));
-        CK(cudaMemsetAsync(head_cnt, 0, nparts * 4, s));
-        CK(cudaMemsetAsync(head_cur, 0, nparts * 4, s));
-        // ---- K2/K3 ----
-        CK(cudaEventRecord(tm.ev[2], s));
-        launch_insert(g, text, lines, reads, n_reads, k, heads, head_cnt, d_st, s);
-        CK(cudaEventRecord(tm.ev[3], s));
-        // ---- K4 + K5a ----
-        exclusive_scan_u32(head_cnt, head_off, nparts, nullptr, pscratch, s);
-        launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, nparts, s);
-        EmitArgs a{};
-        a.g = g;
-        a.k = k;
-        a.text = text;
-        a.lines = lines;
-        a.reads = reads;
-        a.heads = heads;
-        a.head_idx = head_idx;
-        a.head_sk = head_sk;
-        a.head_off = head_off;
-        a.head_cnt = head_cnt;
-        a.head_cnt2 = head_cnt2;
-        a.part_nodes = part_nodes;
-        a.part_bytes = part_bytes;
-        a.part_off = part_off;
-        a.st = d_st;
-        launch_emit_prepare(a, s);
-        exclusive_scan_u64(part_bytes, part_off, nparts, part_off + nparts, pscratch, s);
-        CK(cudaEventRecord(tm.ev[4], s));
-        unsigned long long total = 0;
-        CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(&total, part_off + nparts, 8, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        CK(cudaGetLastError());
-        if (hs.table_full) {
-            cudaFreeAsync(part_off, s);
-            // the upper bound on distinct k-mers is the occurrence count; a full partition
-            // means a skewed hash bucket, so retry with more slots
-            DevStatus zero{};
-            zero.parse_err = ~0ULL;
-            zero.n_reads = hs.n_reads;
-            zero.n_occ = hs.n_occ;
-            CK(cudaMemcpyAsync(d_st, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
-            if (attempt >= 2) return GX_ETABLE_FULL;
-            lf *= 0.5;
-            continue;
-        }
-        // ---- K5b ----
-        void *outp = nullptr;
-        CK(cudaMallocAsync(&outp, total + 16, s));
-        if (((uintptr_t)outp & 15) != 0) {  // the record writer stores aligned 16-byte vectors
-            cudaFreeAsync(outp, s);
-            cudaFreeAsync(part_off, s);
-            return GX_ECUDA;
-        }
-        a.out = (uint8_t *)outp;
-        CK(cudaEventRecord(tm.ev[5], s));
-        launch_emit_write(a, s);
-        CK(cudaEventRecord(tm.ev[6], s));
-        CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        CK(cudaGetLastError());
-        if (hs.internal_err) {
-            cudaFreeAsync(outp, s);
-            cudaFreeAsync(part_off, s);
-            fprintf(stderr, "gxgpu: internal error: record sizes disagree between emission passes\n");
-            return GX_ECUDA;
-        }
-        // output parts = contiguous ranges of table partitions
-        const int P = j->o.out_parts;
-        for (int q = 0; q <= P; q++) {
-            const uint64_t tp = (uint64_t)nparts * q / P;
-            unsigned long long v = 0;
-            if (q == P)
-                v = total;
-            else if (tp > 0)
-                CK(cudaMemcpy(&v, part_off + tp, 8, cudaMemcpyDeviceToHost));
-            j->part_bounds[q] = v;
-        }
-        for (int q = 0; q < P; q++) j->cursor[q] = j->part_bounds[q];
-        // node and read-head totals
-        {
-            std::vector<uint32_t> pn(nparts), hc(nparts);
-            CK(cudaMemcpy(pn.data(), part_nodes, nparts * 4, cudaMemcpyDeviceToHost));
-            CK(cudaMemcpy(hc.data(), head_cnt2, nparts * 4, cudaMemcpyDeviceToHost));
-            uint64_t nn = 0, nh = 0;
-            for (uint32_t q = 0; q < nparts; q++) {
-                nn += pn[q];
-                nh += hc[q];
-            }
-            j->st.nodes = nn;
-            j->st.read_heads = nh;
-        }
-        j->d_out = (uint8_t *)outp;
-        j->out_bytes = total;
-        j->d_part_off = part_off;
-        j->nparts = nparts;
-        j->st.record_bytes = total;
-        j->st.table_slots = (uint64_t)nparts * PART_SLOTS;
-        j->st.table_partitions = nparts;
-        j->st.max_probe = hs.max_probe;
-        j->st.cov_inexact_nodes = hs.cov_inexact;
-        j->st.ms_insert = tm.ms(2, 3);
-        j->st.ms_emit = tm.ms(3, 4) + tm.ms(5, 6);
-        j->st.ms_total = tm.ms(0, 6);
-        break;
-    }
-    return GX_OK;
+    rc.n_reads = n_reads;
+    rc.n_occ = hs.n_occ;
+    return partitioned ? build_partitioned(rc) : build_table(rc);
 }

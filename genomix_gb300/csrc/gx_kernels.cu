@@ -7,6 +7,8 @@
 //   K4  read-head bucketing + sort     ReadHeadSet / ExternalableTreeSet.union (:138-145)
 //   K5  compaction + serialization     outputFinalResult (:185-214), Node.write,
 //                                      KmerNodePairSequenceWriterFactory.write (:79-94)
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 
 #include "gx_kernels.cuh"
@@ -408,7 +410,7 @@ void launch_parse_lines(const uint8_t *text, uint64_t n_text, const unsigned lon
     if (!n_lines) return;
     const uint64_t warps = n_lines;
     uint64_t blocks = (warps * 32 + 255) / 256;
-    if (blocks > 152ull * 64) blocks = 152ull * 64;
+    if (blocks > 0x7fffffffULL) blocks = 0x7fffffffULL;
     t_launches++;
     k_parse_lines<<<(unsigned)blocks, 256, 0, s>>>(text, n_text, line_end, n_lines, k, lines, lflags, nvalid, st);
 }
@@ -506,6 +508,8 @@ __global__ void __launch_bounds__(256) k_insert(typename SlotOf<K>::T *table, ui
                 hd.slot = (uint32_t)si;
                 hd.uuid = ((unsigned long long)(d == 0 ? 0 : k - 1) << 40) | ((unsigned long long)mate << 35) |
                           (unsigned long long)lr.read_id;
+                hd.klo = (unsigned long long)canon;
+                hd.khi = (unsigned long long)((u128)canon >> 64);
                 heads[r] = hd;
                 if (si >= 0) atomicAdd(&head_cnt[p], 1u);
             }
@@ -564,18 +568,23 @@ void launch_head_scatter(const Head *heads, uint32_t n_reads, const uint32_t *he
 // Ascending-only bitonic network over (key, val) pairs with virtual +inf past n.
 template <class KT, class VT>
 __device__ void bitonic_sort_pairs(KT *key, VT *val, uint32_t n) {
-    uint32_t N = 1;
-    while (N < n) N <<= 1;
-    for (uint32_t size = 2; size <= N; size <<= 1) {
-        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+    uint32_t N = 1, logN = 0;
+    while (N < n) {
+        N <<= 1;
+        logN++;
+    }
+    for (uint32_t ls = 1; ls <= logN; ls++) {
+        const uint32_t size = 1u << ls;
+        for (uint32_t lt = ls; lt-- > 0;) {
+            const uint32_t stride = 1u << lt;
             for (uint32_t i = threadIdx.x; i < N / 2; i += blockDim.x) {
-                const uint32_t blk = i / stride, off = i % stride;
+                const uint32_t blk = i >> lt, off = i & (stride - 1);
                 uint32_t lo, hi;
-                if (stride == (size >> 1)) {
-                    lo = blk * size + off;
-                    hi = blk * size + size - 1 - off;
+                if (lt == ls - 1) {
+                    lo = (blk << ls) + off;
+                    hi = (blk << ls) + size - 1 - off;
                 } else {
-                    lo = blk * 2 * stride + off;
+                    lo = (blk << (lt + 1)) + off;
                     hi = lo + stride;
                 }
                 if (hi < n) {
@@ -898,7 +907,17 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_write(EmitArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     // nodes: up to PART_SLOTS / EMIT_THREADS independent loads per thread
     constexpr int PER = PART_SLOTS / EMIT_THREADS;
-    {
+    if (a.nkey) {
+        // partitioned build: compacted nodes in (key, count | meta << 32) arrays
+        const K *nk = (const K *)a.nkey + a.node_base[p];
+        const unsigned long long *ncm = a.ncm + a.node_base[p];
+        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+            sm.key[j] = nk[j];
+            const unsigned long long cm = ncm[j];
+            sm.cnt[j] = (uint32_t)cm;
+            sm.meta[j] = (uint32_t)(cm >> 32);
+        }
+    } else {
         K kk[PER];
         uint32_t cc[PER], mm[PER];
         bool oo[PER];
@@ -1151,6 +1170,1085 @@ void launch_emit_write(const EmitArgs &a, cudaStream_t s) {
         cudaFuncSetAttribute(k_emit_write<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         t_launches++;
         k_emit_write<uint64_t><<<a.g.nparts, EMIT_THREADS, sm, s>>>(a);
+    }
+}
+
+
+// =========================================================================================
+// Partitioned build.  Every occurrence is streamed twice through shared-memory counting
+// sorts (super bucket, then fine bucket), then each fine bucket is aggregated by one CTA in
+// a shared-memory hash table: no random DRAM access, no global table.
+//   A1  occurrence counts per super bucket + HyperLogLog of the canonical k-mers
+//   A2  occurrences -> super buckets              (key, 16 edge bits)
+//   B1  counts per fine bucket
+//   B2  super buckets -> fine buckets
+//   C   per fine bucket: shared-memory aggregation, read heads, key sort, record sizes
+// then the record writer (k_emit_write) as in the table build.
+// =========================================================================================
+
+// Rolling walk over the k-mer occurrences of one read (the same arithmetic as k_insert).
+// Letters are read 8 at a time with aligned loads; the letter leaving the window (base j-1
+// for occurrence j) is the low two bits of the previous forward value.
+template <class K>
+struct Walker {
+    const uint8_t *text;
+    unsigned long long n_text, xo;  // next unread letter offset
+    unsigned long long xbuf;
+    uint32_t xn;
+    uint32_t nk, j, yb;
+    int k, sh;
+    K mask, fwd, rc;
+    uint32_t d, pd;
+    __device__ __forceinline__ uint32_t letter() {
+        if (xn == 0) {
+            const unsigned long long al = xo & ~7ULL;
+            if (al + 8 <= n_text) {
+                xbuf = *reinterpret_cast<const unsigned long long *>(text + al) >> (8 * (xo - al));
+                xn = 8 - (uint32_t)(xo - al);
+            } else {
+                xbuf = 0;
+                xn = 0;
+                for (unsigned long long q = xo; q < n_text && xn < 8; q++, xn++) xbuf |= (unsigned long long)text[q] << (8 * xn);
+            }
+        }
+        const uint32_t c = base_code((uint32_t)xbuf & 0xffu);
+        xbuf >>= 8;
+        xn--;
+        xo++;
+        return c;
+    }
+    __device__ __forceinline__ void init(const uint8_t *text_, unsigned long long n_text_, unsigned long long s_off,
+                                         uint32_t L, int k_) {
+        text = text_;
+        n_text = n_text_;
+        xo = s_off;
+        xn = 0;
+        xbuf = 0;
+        k = k_;
+        sh = 2 * (k - 1);
+        mask = KeyOps<K>::mask(k);
+        fwd = 0;
+        rc = 0;
+        for (int i = 0; i < k; i++) {
+            const uint32_t c = letter();
+            fwd = (fwd >> 2) | ((K)c << sh);
+            rc = ((rc << 2) | (K)(3u - c)) & mask;
+        }
+        nk = L - (uint32_t)k + 1;
+        j = 0;
+        d = fwd <= rc ? 0u : 1u;
+        pd = 0;
+        yb = 0;
+    }
+    __device__ __forceinline__ void empty() {
+        nk = 0;
+        j = 0;
+    }
+    __device__ __forceinline__ bool done() const { return j >= nk; }
+    // the current occurrence: canonical value, its <= 2 edge bits, orientation; then advance
+    __device__ __forceinline__ void next(K &canon, uint32_t &bits, uint32_t &dir) {
+        const bool hn = j + 1 < nk;
+        K nf = fwd, nr = rc;
+        uint32_t nd = 0, x = 0;
+        if (hn) {
+            x = letter();
+            nf = (fwd >> 2) | ((K)x << sh);
+            nr = ((rc << 2) | (K)(3u - x)) & mask;
+            nd = nf <= nr ? 0u : 1u;
+        }
+        bits = 0;
+        if (hn) bits |= 1u << (4 * (2 * d + nd) + (d == 0 ? x : 3u - x));
+        if (j > 0) bits |= 1u << (4 * (2 * (d ^ 1u) + (pd ^ 1u)) + (d == 1 ? 3u - yb : yb));
+        canon = d == 0 ? fwd : rc;
+        dir = d;
+        yb = (uint32_t)(fwd & (K)3);
+        pd = d;
+        d = nd;
+        fwd = nf;
+        rc = nr;
+        j++;
+    }
+};
+
+template <class K>
+__device__ __forceinline__ void walker_for(Walker<K> &w, const uint8_t *text, unsigned long long n_text,
+                                           const LineRec *lines, const uint32_t *reads, uint32_t r, int k) {
+    const uint32_t rl = reads[r];
+    const LineRec lr = lines[rl >> 1];
+    const uint32_t mate = rl & 1u;
+    w.init(text, n_text, mate ? lr.s1 : lr.s0, mate ? lr.l1 : lr.l0, k);
+}
+
+__device__ __forceinline__ uint32_t super_of(uint64_t h, uint32_t log_s) { return (uint32_t)(h >> (64 - log_s)); }
+// fine bucket (global index) of a key hash; the 32 hash bits below the super bits pick
+// the fine bucket inside the super bucket; the low bits are left for the table slot
+__device__ __forceinline__ uint32_t fine_of(uint64_t h, const PartPlan &pp) {
+    return super_of(h, pp.log_s) * pp.F + __umulhi((uint32_t)(h >> (32 - pp.log_s)), pp.F);
+}
+
+// Exclusive scan, in place, of a shared array of n <= blockDim * 32 entries; returns the total.
+__device__ uint32_t block_scan_array(uint32_t *a, uint32_t n, uint32_t *ws) {
+    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t t0 = min(n, threadIdx.x * per), t1 = min(n, t0 + per);
+    uint32_t sum = 0;
+    for (uint32_t i = t0; i < t1; i++) sum += a[i];
+    uint32_t tot;
+    uint32_t ex = block_exclusive_scan(sum, ws, tot);
+    for (uint32_t i = t0; i < t1; i++) {
+        const uint32_t v = a[i];
+        a[i] = ex;
+        ex += v;
+    }
+    __syncthreads();
+    return tot;
+}
+
+// ---- A1 -------------------------------------------------------------------------------------
+template <class K>
+__global__ void __launch_bounds__(256) k_count_occ(const uint8_t *text, unsigned long long n_text,
+                                                   const LineRec *lines, const uint32_t *reads,
+                                                   const uint32_t *n_reads_dev, int k, uint32_t log_s,
+                                                   uint32_t *s_cnt, uint32_t *hll) {
+    __shared__ uint32_t hist[MAX_SUPERS];
+    __shared__ uint32_t reg[HLL_REGS];
+    const uint32_t S = 1u << log_s;
+    for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) hist[i] = 0;
+    for (uint32_t i = threadIdx.x; i < HLL_REGS; i += blockDim.x) reg[i] = 0;
+    __syncthreads();
+    const uint32_t n_reads = *n_reads_dev;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += gridDim.x * blockDim.x) {
+        Walker<K> w;
+        walker_for(w, text, n_text, lines, reads, r, k);
+        while (!w.done()) {
+            K c;
+            uint32_t b, d;
+            w.next(c, b, d);
+            const uint64_t h = KeyOps<K>::hash(c);
+            atomicAdd(&hist[super_of(h, log_s)], 1u);
+            const uint64_t w2 = h >> 11;  // HyperLogLog: register = low 11 bits, rank of the rest
+            const uint32_t rho = w2 ? (uint32_t)(__clzll(w2) - 10) : 54u;
+            atomicMax(&reg[h & (HLL_REGS - 1)], rho);
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < S; i += blockDim.x)
+        if (hist[i]) atomicAdd(&s_cnt[i], hist[i]);
+    for (uint32_t i = threadIdx.x; i < HLL_REGS; i += blockDim.x)
+        if (reg[i]) atomicMax(&hll[i], reg[i]);
+}
+
+// HyperLogLog (Flajolet, Fusy, Gandouet, Meunier 2007) with the small-range correction
+double hll_estimate(const uint32_t *regs) {
+    const double m = HLL_REGS;
+    double z = 0;
+    int zeros = 0;
+    for (int i = 0; i < HLL_REGS; i++) {
+        z += ldexp(1.0, -(int)regs[i]);
+        if (regs[i] == 0) zeros++;
+    }
+    const double alpha = 0.7213 / (1.0 + 1.079 / m);
+    double e = alpha * m * m / z;
+    if (e <= 2.5 * m && zeros > 0) e = m * log(m / zeros);
+    return e;
+}
+
+PartPlan plan_partitions(double distinct_est, double safety, double target) {
+    double want = distinct_est * safety / target;
+    if (want < 1) want = 1;
+    uint64_t P = (uint64_t)ceil(want);
+    uint32_t log_s = 0;
+    while ((1ull << (2 * log_s)) < P && log_s < 11) log_s++;  // S ~ sqrt(P)
+    if (log_s < 6) log_s = 6;
+    const uint64_t S = 1ull << log_s;
+    uint64_t F = (P + S - 1) / S;
+    if (F < 1) F = 1;
+    if (F > MAX_FINE) F = MAX_FINE;
+    PartPlan pp;
+    pp.log_s = log_s;
+    pp.F = (uint32_t)F;
+    pp.P = (uint32_t)(S * F);
+    return pp;
+}
+
+void launch_count_occ(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines, const uint32_t *reads,
+                      const uint32_t *n_reads_dev, uint32_t n_reads_max, int k, uint32_t log_s, uint32_t *s_cnt,
+                      uint32_t *hll, cudaStream_t s) {
+    if (!n_reads_max) return;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((n_reads_max + 255) / 256, 152ull * 8);
+    t_launches++;
+    if (wide)
+        k_count_occ<u128><<<blocks, 256, 0, s>>>(text, n_text, lines, reads, n_reads_dev, k, log_s, s_cnt, hll);
+    else
+        k_count_occ<uint64_t><<<blocks, 256, 0, s>>>(text, n_text, lines, reads, n_reads_dev, k, log_s, s_cnt,
+                                                     hll);
+}
+
+// ---- A2 -------------------------------------------------------------------------------------
+// shared layout of k_scatter_super: staging for one round, then three S-entry arrays
+template <class K>
+struct SuperSmem {
+    K key[SC_THREADS * SC_ROUND];
+    uint16_t bits[SC_THREADS * SC_ROUND];
+    uint16_t sup[SC_THREADS * SC_ROUND];
+    uint32_t ws[33];
+    uint32_t rounds, total;
+    uint32_t arrays[1];  // loff[S], gbase[S], cur[S]
+    static size_t bytes(uint32_t S) { return sizeof(SuperSmem) + 3ull * S * sizeof(uint32_t); }
+};
+
+template <class K>
+__global__ void __launch_bounds__(SC_THREADS) k_scatter_super(const uint8_t *text, unsigned long long n_text,
+                                                              const LineRec *lines,
+                                                              const uint32_t *reads, uint32_t n_reads, int k,
+                                                              uint32_t log_s, const unsigned long long *s_off,
+                                                              uint32_t *s_cur, K *okey, uint16_t *obits) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    SuperSmem<K> &sm = *reinterpret_cast<SuperSmem<K> *>(smem_raw);
+    const uint32_t S = 1u << log_s;
+    uint32_t *const sm_loff = sm.arrays, *const sm_gbase = sm.arrays + S, *const sm_cur = sm.arrays + 2 * S;
+    const uint32_t r = blockIdx.x * SC_THREADS + threadIdx.x;
+    Walker<K> w;
+    if (r < n_reads)
+        walker_for(w, text, n_text, lines, reads, r, k);
+    else
+        w.empty();
+    if (threadIdx.x == 0) sm.rounds = 0;
+    __syncthreads();
+    atomicMax(&sm.rounds, (w.nk + SC_ROUND - 1) / SC_ROUND);
+    __syncthreads();
+    const uint32_t rounds = sm.rounds;
+    for (uint32_t round = 0; round < rounds; round++) {
+        for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) sm_cur[i] = 0;
+        __syncthreads();
+        const Walker<K> w0 = w;
+        // count this round's occurrences per super bucket
+        for (int q = 0; q < SC_ROUND && !w.done(); q++) {
+            K c;
+            uint32_t b, d;
+            w.next(c, b, d);
+            atomicAdd(&sm_cur[super_of(KeyOps<K>::hash(c), log_s)], 1u);
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) {
+            sm_loff[i] = sm_cur[i];
+            sm_gbase[i] = sm_cur[i] ? atomicAdd(&s_cur[i], sm_cur[i]) : 0u;
+        }
+        __syncthreads();
+        const uint32_t tot = block_scan_array(sm_loff, S, sm.ws);
+        for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) sm_cur[i] = 0;
+        __syncthreads();
+        // place them in shared memory grouped by super bucket
+        w = w0;
+        for (int q = 0; q < SC_ROUND && !w.done(); q++) {
+            K c;
+            uint32_t b, d;
+            w.next(c, b, d);
+            const uint32_t sp = super_of(KeyOps<K>::hash(c), log_s);
+            const uint32_t pos = sm_loff[sp] + atomicAdd(&sm_cur[sp], 1u);
+            sm.key[pos] = c;
+            sm.bits[pos] = (uint16_t)b;
+            sm.sup[pos] = (uint16_t)sp;
+        }
+        __syncthreads();
+        // write the runs out
+        for (uint32_t i = threadIdx.x; i < tot; i += blockDim.x) {
+            const uint32_t sp = sm.sup[i];
+            const unsigned long long g = s_off[sp] + sm_gbase[sp] + (i - sm_loff[sp]);
+            okey[g] = sm.key[i];
+            obits[g] = sm.bits[i];
+        }
+        __syncthreads();
+    }
+}
+
+void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
+                          const uint32_t *reads, uint32_t n_reads, int k, uint32_t log_s, const unsigned long long *s_off, uint32_t *s_cur,
+                          void *okey, uint16_t *obits, cudaStream_t s) {
+    if (!n_reads) return;
+    const unsigned blocks = (n_reads + SC_THREADS - 1) / SC_THREADS;
+    t_launches++;
+    if (wide) {
+        const size_t sm = SuperSmem<u128>::bytes(1u << log_s);
+        cudaFuncSetAttribute(k_scatter_super<u128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_scatter_super<u128><<<blocks, SC_THREADS, sm, s>>>(text, n_text, lines, reads, n_reads, k, log_s, s_off,
+                                                             s_cur, (u128 *)okey, obits);
+    } else {
+        const size_t sm = SuperSmem<uint64_t>::bytes(1u << log_s);
+        cudaFuncSetAttribute(k_scatter_super<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_scatter_super<uint64_t><<<blocks, SC_THREADS, sm, s>>>(text, n_text, lines, reads, n_reads, k, log_s,
+                                                                 s_off, s_cur, (uint64_t *)okey, obits);
+    }
+}
+
+// ---- B1 -------------------------------------------------------------------------------------
+template <class K>
+__global__ void __launch_bounds__(256) k_fine_count(const K *okey, const ulonglong2 *chunks, PartPlan pp,
+                                                    unsigned long long *fine_cnt) {
+    __shared__ uint32_t bins[MAX_FINE];
+    const ulonglong2 ch = chunks[blockIdx.x];
+    const uint32_t sp = (uint32_t)(ch.y >> 32), len = (uint32_t)ch.y;
+    for (uint32_t i = threadIdx.x; i < pp.F; i += blockDim.x) bins[i] = 0;
+    __syncthreads();
+    const uint32_t f0 = sp * pp.F;
+    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x)
+        atomicAdd(&bins[fine_of(KeyOps<K>::hash(okey[ch.x + i]), pp) - f0], 1u);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < pp.F; i += blockDim.x)
+        if (bins[i]) atomicAdd(&fine_cnt[f0 + i], (unsigned long long)bins[i]);
+}
+
+void launch_fine_count(int wide, const void *okey, const ulonglong2 *chunks, uint32_t n_chunks, PartPlan pp,
+                       unsigned long long *fine_cnt, cudaStream_t s) {
+    if (!n_chunks) return;
+    t_launches++;
+    if (wide)
+        k_fine_count<u128><<<n_chunks, 256, 0, s>>>((const u128 *)okey, chunks, pp, fine_cnt);
+    else
+        k_fine_count<uint64_t><<<n_chunks, 256, 0, s>>>((const uint64_t *)okey, chunks, pp, fine_cnt);
+}
+
+// ---- B2 -------------------------------------------------------------------------------------
+template <class K>
+struct FineSmem {
+    K key[CHUNK];
+    uint16_t bits[CHUNK];
+    uint32_t loff[MAX_FINE];
+    uint32_t gbase[MAX_FINE];
+    uint32_t cur[MAX_FINE];
+    uint32_t ws[33];
+};
+
+template <class K>
+__global__ void __launch_bounds__(256) k_scatter_fine(const K *okey, const uint16_t *obits, const ulonglong2 *chunks,
+                                                      PartPlan pp, const unsigned long long *fine_off,
+                                                      uint32_t *fine_cur, K *okey2, uint16_t *obits2) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    FineSmem<K> &sm = *reinterpret_cast<FineSmem<K> *>(smem_raw);
+    const ulonglong2 ch = chunks[blockIdx.x];
+    const uint32_t sp = (uint32_t)(ch.y >> 32), len = (uint32_t)ch.y;
+    const uint32_t f0 = sp * pp.F, F = pp.F;
+    for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) sm.cur[i] = 0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x)
+        atomicAdd(&sm.cur[fine_of(KeyOps<K>::hash(okey[ch.x + i]), pp) - f0], 1u);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) {
+        sm.loff[i] = sm.cur[i];
+        sm.gbase[i] = sm.cur[i] ? atomicAdd(&fine_cur[f0 + i], sm.cur[i]) : 0u;
+    }
+    __syncthreads();
+    block_scan_array(sm.loff, F, sm.ws);
+    for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) sm.cur[i] = 0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
+        const K key = okey[ch.x + i];
+        const uint32_t b = fine_of(KeyOps<K>::hash(key), pp) - f0;
+        const uint32_t pos = sm.loff[b] + atomicAdd(&sm.cur[b], 1u);
+        sm.key[pos] = key;
+        sm.bits[pos] = obits[ch.x + i];
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
+        const K key = sm.key[i];
+        const uint32_t b = fine_of(KeyOps<K>::hash(key), pp) - f0;
+        const unsigned long long g = fine_off[f0 + b] + sm.gbase[b] + (i - sm.loff[b]);
+        okey2[g] = key;
+        obits2[g] = sm.bits[i];
+    }
+}
+
+void launch_scatter_fine(int wide, const void *okey, const uint16_t *obits, const ulonglong2 *chunks,
+                         uint32_t n_chunks, PartPlan pp, const unsigned long long *fine_off, uint32_t *fine_cur,
+                         void *okey2, uint16_t *obits2, cudaStream_t s) {
+    if (!n_chunks) return;
+    t_launches++;
+    if (wide) {
+        const size_t sm = sizeof(FineSmem<u128>);
+        cudaFuncSetAttribute(k_scatter_fine<u128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_scatter_fine<u128><<<n_chunks, 256, sm, s>>>((const u128 *)okey, obits, chunks, pp, fine_off, fine_cur,
+                                                      (u128 *)okey2, obits2);
+    } else {
+        const size_t sm = sizeof(FineSmem<uint64_t>);
+        cudaFuncSetAttribute(k_scatter_fine<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_scatter_fine<uint64_t><<<n_chunks, 256, sm, s>>>((const uint64_t *)okey, obits, chunks, pp, fine_off,
+                                                          fine_cur, (uint64_t *)okey2, obits2);
+    }
+}
+
+// ---- read heads (partitioned build) ----------------------------------------------------------
+template <class K>
+__global__ void k_heads_part(const uint8_t *text, unsigned long long n_text, const LineRec *lines,
+                             const uint32_t *reads, uint32_t n_reads,
+                             int k, PartPlan pp, Head *heads, uint32_t *head_cnt) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_reads) return;
+    Walker<K> w;
+    walker_for(w, text, n_text, lines, reads, r, k);
+    K c;
+    uint32_t b, d;
+    w.next(c, b, d);
+    const uint32_t mate = reads[r] & 1u;
+    const long long rid = lines[reads[r] >> 1].read_id;
+    const uint32_t f = fine_of(KeyOps<K>::hash(c), pp);
+    Head hd;
+    hd.part = f;
+    hd.slot = 0;
+    hd.uuid = ((unsigned long long)(d == 0 ? 0 : k - 1) << 40) | ((unsigned long long)mate << 35) |
+              (unsigned long long)rid;
+    hd.klo = (unsigned long long)c;
+    hd.khi = (unsigned long long)((u128)c >> 64);
+    heads[r] = hd;
+    atomicAdd(&head_cnt[f], 1u);
+}
+
+void launch_heads_part(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines, const uint32_t *reads,
+                       uint32_t n_reads, int k, PartPlan pp, Head *heads, uint32_t *head_cnt, cudaStream_t s) {
+    if (!n_reads) return;
+    t_launches++;
+    if (wide)
+        k_heads_part<u128><<<(n_reads + 255) / 256, 256, 0, s>>>(text, n_text, lines, reads, n_reads, k, pp, heads,
+                                                                head_cnt);
+    else
+        k_heads_part<uint64_t><<<(n_reads + 255) / 256, 256, 0, s>>>(text, n_text, lines, reads, n_reads, k, pp,
+                                                                    heads, head_cnt);
+}
+
+// ---- C --------------------------------------------------------------------------------------
+template <class K> struct AggTable;
+template <> struct AggTable<uint64_t> {
+    // stored key = V + 1, 0 = empty; every probe is a CAS so a racing claim is never missed
+    __device__ __forceinline__ static int insert(uint64_t *key1, uint64_t key, uint32_t h, uint32_t &claimed) {
+        const unsigned long long want = (unsigned long long)key + 1ULL;
+        uint32_t i = h & (AGG_SLOTS - 1);
+        for (uint32_t n = 0; n < AGG_SLOTS; n++) {
+            unsigned long long cur = ((volatile unsigned long long *)key1)[i];
+            if (cur != want) cur = atomicCAS((unsigned long long *)&key1[i], 0ULL, want);
+            if (cur == 0ULL) claimed = 1;
+            if (cur == 0ULL || cur == want) return (int)i;
+            i = (i + 1) & (AGG_SLOTS - 1);
+        }
+        return -1;
+    }
+    __device__ __forceinline__ static int find(const uint64_t *key1, uint64_t key, uint32_t h) {
+        const uint64_t want = key + 1;
+        uint32_t i = h & (AGG_SLOTS - 1);
+        for (uint32_t n = 0; n < AGG_SLOTS; n++) {
+            const uint64_t cur = key1[i];
+            if (cur == want) return (int)i;
+            if (cur == 0) return -1;
+            i = (i + 1) & (AGG_SLOTS - 1);
+        }
+        return -1;
+    }
+};
+template <> struct AggTable<u128> {
+    __device__ __forceinline__ static int insert(u128 *key1, u128 key, uint32_t h, uint32_t &claimed) {
+        const u128 want = key + 1;
+        const unsigned long long wlo = (unsigned long long)want, whi = (unsigned long long)(want >> 64);
+        uint32_t i = h & (AGG_SLOTS - 1);
+        for (uint32_t n = 0; n < AGG_SLOTS; n++) {
+            unsigned long long clo, chi;
+            cas128_shared(&key1[i], 0ULL, 0ULL, wlo, whi, clo, chi);
+            if (clo == 0ULL && chi == 0ULL) claimed = 1;
+            if ((clo == 0ULL && chi == 0ULL) || (clo == wlo && chi == whi)) return (int)i;
+            i = (i + 1) & (AGG_SLOTS - 1);
+        }
+        return -1;
+    }
+    __device__ __forceinline__ static int find(const u128 *key1, u128 key, uint32_t h) {
+        const u128 want = key + 1;
+        uint32_t i = h & (AGG_SLOTS - 1);
+        for (uint32_t n = 0; n < AGG_SLOTS; n++) {
+            const u128 cur = key1[i];
+            if (cur == want) return (int)i;
+            if (cur == 0) return -1;
+            i = (i + 1) & (AGG_SLOTS - 1);
+        }
+        return -1;
+    }
+};
+
+template <class K>
+struct AggSmem {
+    K key1[AGG_SLOTS];
+    uint32_t cnt[AGG_SLOTS];
+    uint32_t meta[AGG_SLOTS];
+    uint32_t nbytes[AGG_SLOTS];   // record bytes per node, then its offset
+    uint16_t ord[AGG_SLOTS];
+    uint16_t rank_of_slot[AGG_SLOTS];
+    uint32_t cu[AGG_SLOTS], cf[AGG_SLOTS];  // unflipped / flipped heads per node
+    uint32_t hstart[AGG_SLOTS];   // first kept head of each node
+    unsigned long long ws[33];
+    unsigned long long carry;
+    uint32_t n, fail, kept;
+};
+
+constexpr int AGG_BATCH = 8;  // occurrence loads in flight per thread
+
+template <class K>
+__global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    AggSmem<K> &sm = *reinterpret_cast<AggSmem<K> *>(smem_raw);
+    const uint32_t f = blockIdx.x;
+    const int nb = (a.k + 3) / 4;
+    const unsigned long long o0 = a.fine_off[f], o1 = a.fine_off[f + 1];
+    const K *okey = (const K *)a.okey2 + o0;
+    const uint16_t *obits = a.obits2 + o0;
+    const uint32_t M = (uint32_t)(o1 - o0);
+    for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x) {
+        sm.key1[i] = 0;
+        sm.cnt[i] = 0;
+        sm.meta[i] = 0;
+        sm.nbytes[i] = 0;
+        sm.cu[i] = 0;
+        sm.cf[i] = 0;
+        sm.hstart[i] = 0xffffffffu;
+    }
+    if (threadIdx.x == 0) {
+        sm.n = 0;
+        sm.fail = 0;
+    }
+    __syncthreads();
+    // 1. aggregate the bucket's occurrences: count += 1, edge mask |= bits; each thread
+    //    loads AGG_BATCH occurrences before inserting any of them
+    for (uint32_t c0 = 0; c0 < M; c0 += AGG_BATCH * blockDim.x) {
+        K kk[AGG_BATCH];
+        uint32_t bb[AGG_BATCH];
+#pragma unroll
+        for (int q = 0; q < AGG_BATCH; q++) {
+            const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
+            kk[q] = i < M ? okey[i] : (K)0;
+            bb[q] = i < M ? (uint32_t)obits[i] : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < AGG_BATCH; q++) {
+            const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
+            if (i >= M) continue;
+            uint32_t claimed = 0;
+            const int sl = AggTable<K>::insert(sm.key1, kk[q], (uint32_t)KeyOps<K>::hash(kk[q]), claimed);
+            if (sl < 0) {
+                sm.fail = 1;
+                continue;
+            }
+            if (claimed) atomicAdd(&sm.n, 1u);
+            atomicAdd(&sm.cnt[sl], 1u);
+            if (bb[q]) atomicOr(&sm.meta[sl], bb[q]);
+        }
+    }
+    __syncthreads();
+    if (sm.fail) {
+        if (threadIdx.x == 0) atomicAdd(&a.st->table_full, 1u);
+        return;
+    }
+    // 2. read heads: find their node, mark the unflipped / flipped set
+    const uint32_t hb = a.head_off[f], hc = a.head_cnt[f];
+    for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
+        const uint32_t r = a.head_idx[hb + i];
+        Head h = a.heads[r];
+        const K key = (K)(((u128)h.khi << 64) | h.klo);
+        const int sl = AggTable<K>::find(sm.key1, key, (uint32_t)KeyOps<K>::hash(key));
+        if (sl < 0) {
+            atomicAdd(&a.st->internal_err, 1u);
+            continue;
+        }
+        atomicOr(&sm.meta[sl], (h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
+        h.slot = (uint32_t)sl;
+        a.heads[r] = h;
+    }
+    __syncthreads();
+    // 3. order the nodes deterministically: by home slot (the low hash bits that started the
+    //    probe), then by key: a counting sort over the 2048 home slots; a home holds one or
+    //    two keys at this load, ordered by the thread that owns the home
+    for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x) {
+        const K k1 = sm.key1[i];
+        if (k1 != (K)0) atomicAdd(&sm.cu[(uint32_t)KeyOps<K>::hash(k1 - 1) & (AGG_SLOTS - 1)], 1u);
+    }
+    __syncthreads();
+    block_scan_array(sm.cu, AGG_SLOTS, reinterpret_cast<uint32_t *>(sm.ws));
+    for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x) {
+        const K k1 = sm.key1[i];
+        if (k1 == (K)0) continue;
+        const uint32_t hm = (uint32_t)KeyOps<K>::hash(k1 - 1) & (AGG_SLOTS - 1);
+        sm.ord[sm.cu[hm] + atomicAdd(&sm.cf[hm], 1u)] = (uint16_t)i;
+    }
+    __syncthreads();
+    for (uint32_t hm = threadIdx.x; hm < AGG_SLOTS; hm += blockDim.x) {
+        const uint32_t b0 = sm.cu[hm], c = sm.cf[hm];
+        for (uint32_t u = 1; u < c; u++)
+            for (uint32_t v = b0 + u; v > b0 && sm.key1[sm.ord[v]] < sm.key1[sm.ord[v - 1]]; v--) {
+                const uint16_t t = sm.ord[v];
+                sm.ord[v] = sm.ord[v - 1];
+                sm.ord[v - 1] = t;
+            }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x) {
+        sm.cu[i] = 0;
+        sm.cf[i] = 0;
+    }
+    const uint32_t n = sm.n;
+    __syncthreads();
+    // 4. nodes out (over the bucket's own occurrence range); record bytes without heads
+    K *nkey = (K *)a.nkey + o0;
+    unsigned long long *ncm = a.ncm + o0;
+    uint32_t inexact = 0;
+    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+        const uint32_t o = sm.ord[j];
+        sm.rank_of_slot[o] = (uint16_t)j;
+        nkey[j] = sm.key1[o] - 1;
+        ncm[j] = (unsigned long long)sm.cnt[o] | ((unsigned long long)sm.meta[o] << 32);
+        if (sm.cnt[o] >= (1u << 24)) inexact++;
+    }
+    if (inexact) atomicAdd(&a.st->cov_inexact, inexact);
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) sm.nbytes[j] = node_base_bytes(sm.meta[sm.ord[j]], nb);
+    // 5. read heads: sort by (node, TreeSet order), keep the first of equal uuids
+    // (the sort runs in global scratch: a bucket holds few heads)
+    unsigned long long *hk = a.head_sk + hb;
+    uint32_t *hv = a.head_idx + hb;
+    if (hc > HEAD_CAP && threadIdx.x == 0) atomicAdd(&a.st->big_head_parts, 1u);
+    for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
+        const uint32_t r = hv[i];
+        const Head h = a.heads[r];
+        hk[i] = head_sort_key(sm.rank_of_slot[h.slot], h.uuid);
+    }
+    __syncthreads();
+    bitonic_sort_pairs<unsigned long long, uint32_t>(hk, hv, hc);
+    if (threadIdx.x == 0) {
+        sm.kept = 0;
+        sm.carry = 0;
+    }
+    __syncthreads();
+    for (uint32_t c0 = 0; c0 < hc; c0 += blockDim.x) {
+        const uint32_t i = c0 + threadIdx.x;
+        unsigned long long key = 0;
+        uint32_t keep = 0, r = 0;
+        if (i < hc) {
+            key = hk[i];
+            const unsigned long long prev = i == 0 ? ~0ULL : (i == c0 ? sm.carry : hk[i - 1]);
+            keep = key != prev ? 1u : 0u;
+            r = hv[i];
+        }
+        const unsigned long long last = hk[min(hc, c0 + blockDim.x) - 1];
+        unsigned long long tot;
+        const unsigned long long ex = block_exclusive_scan((unsigned long long)keep, sm.ws, tot);
+        if (keep) {
+            const uint32_t w = sm.kept + (uint32_t)ex;
+            hk[w] = key;
+            hv[w] = r;
+            const uint32_t rank = (uint32_t)(key >> 37);
+            const uint32_t rl = a.reads[r];
+            atomicAdd(&sm.nbytes[rank], head_bytes(a.lines[rl >> 1], rl & 1u));
+            if ((key >> 36) & 1ULL)
+                atomicAdd(&sm.cf[rank], 1u);
+            else
+                atomicAdd(&sm.cu[rank], 1u);
+            atomicMin(&sm.hstart[rank], w);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            sm.kept += (uint32_t)tot;
+            sm.carry = last;
+        }
+        __syncthreads();
+    }
+    const uint32_t kept = sm.kept;
+    // 6. record offsets of the nodes in the partition
+    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t t0 = min(n, threadIdx.x * per), t1 = min(n, t0 + per);
+    unsigned long long mine = 0;
+    for (uint32_t j = t0; j < t1; j++) mine += sm.nbytes[j];
+    unsigned long long tot_bytes;
+    unsigned long long run = block_exclusive_scan(mine, sm.ws, tot_bytes);
+    uint32_t *noff = a.noff + o0;
+    for (uint32_t j = t0; j < t1; j++) {
+        const uint32_t b = sm.nbytes[j];
+        sm.nbytes[j] = (uint32_t)run;
+        noff[j] = (uint32_t)run;
+        run += b;
+    }
+    __syncthreads();
+    // 7. byte position of every kept head: node offset, frame + key + active + edges, the
+    //    set headers, the heads of the node before it
+    HeadOut *hout = a.hout + hb;
+    const uint32_t keylen = 4 + nb;
+    unsigned long long hrun = 0;
+    for (uint32_t c0 = 0; c0 < kept; c0 += blockDim.x) {
+        const uint32_t i = c0 + threadIdx.x;
+        uint32_t hsz = 0, r = 0, rl = 0;
+        LineRec lr{};
+        if (i < kept) {
+            r = hv[i];
+            rl = a.reads[r];
+            lr = a.lines[rl >> 1];
+            hsz = head_bytes(lr, rl & 1u);
+        }
+        unsigned long long tot;
+        const unsigned long long ex = block_exclusive_scan((unsigned long long)hsz, sm.ws, tot);
+        // the running byte count of kept heads: stash each head's prefix in hk's low bits
+        if (i < kept) {
+            const unsigned long long pre = hrun + ex;
+            const unsigned long long key = hk[i];
+            hk[i] = (key & ~((1ULL << 36) - 1)) | pre;  // rank << 37 | flipped << 36 | prefix
+        }
+        hrun += tot;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
+        const unsigned long long key = hk[i];
+        const uint32_t rank = (uint32_t)(key >> 37);
+        const bool flipped = (key >> 36) & 1ULL;
+        const uint32_t st = sm.hstart[rank];
+        const unsigned long long pre = key & ((1ULL << 36) - 1);
+        const unsigned long long pre0 = hk[st] & ((1ULL << 36) - 1);
+        const uint32_t meta = sm.meta[sm.ord[rank]];
+        const uint32_t cu = sm.cu[rank], cf = sm.cf[rank];
+        uint32_t edges = 0;
+        for (int t = 0; t < 4; t++) {
+            const uint32_t m = (meta >> (4 * t)) & 15u;
+            if (m) edges += 4 + __popc(m) * (4 + nb);
+        }
+        const uint32_t pos = sm.nbytes[rank] + 8 + keylen + 1 + edges + 5 + ((flipped && cu > 0) ? 5 : 0) +
+                             (uint32_t)(pre - pre0);
+        const uint32_t r = hv[i];
+        const uint32_t rl = a.reads[r];
+        const LineRec lr = a.lines[rl >> 1];
+        const uint32_t mate = rl & 1u;
+        HeadOut ho;
+        ho.uuid = a.heads[r].uuid;
+        ho.s_off = mate ? lr.s1 : lr.s0;
+        ho.m_off = mate ? lr.s0 : lr.s1;
+        ho.L = mate ? lr.l1 : lr.l0;
+        ho.Lm = mate ? lr.l0 : lr.l1;
+        ho.pos = pos;
+        ho.set_count = (i == st && !flipped) ? cu : ((flipped && i == st + cu) ? cf : 0u);
+        hout[i] = ho;
+    }
+    if (threadIdx.x == 0) {
+        a.part_nodes[f] = n;
+        a.part_bytes[f] = tot_bytes;
+        a.head_cnt2[f] = kept;
+    }
+}
+
+void launch_aggregate(const AggArgs &a, cudaStream_t s) {
+    if (!a.pp.P) return;
+    t_launches++;
+    if (a.wide) {
+        const size_t sm = sizeof(AggSmem<u128>);
+        cudaFuncSetAttribute(k_aggregate<u128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_aggregate<u128><<<a.pp.P, 256, sm, s>>>(a);
+    } else {
+        const size_t sm = sizeof(AggSmem<uint64_t>);
+        cudaFuncSetAttribute(k_aggregate<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_aggregate<uint64_t><<<a.pp.P, 256, sm, s>>>(a);
+    }
+}
+
+// ---- D: record writer of the partitioned build ------------------------------------------------
+// Each warp writes the records of a contiguous node range through a private window of
+// shared memory; node offsets and read-head positions come precomputed, so no block-wide
+// barrier is needed.  A node lane writes frame, key, active byte, edges and coverage with
+// whole-word stores (WordWriter); the read-head sets are written warp-cooperatively.
+constexpr uint32_t WARP_STAGE = 6144;
+constexpr int WRITER_WARPS = 8;
+
+// Big-endian fields at byte positions of a shared window.  A record's words are stored
+// whole; the word it shares with its predecessor (its first word, when it starts mid-word)
+// and the word it shares with its successor (its trailing partial word) are merged with
+// atomicOr into words zeroed beforehand.
+struct WordWriter {
+    uint32_t *w;
+    uint32_t pos;    // next byte position (window-relative)
+    uint32_t cur;    // pending bytes of word pos >> 2, in memory order from the low byte
+    bool merge_first;  // the next word flushed is shared with the predecessor
+    __device__ __forceinline__ void begin(uint32_t *w_, uint32_t p, bool shared_start) {
+        w = w_;
+        pos = p;
+        cur = 0;
+        merge_first = shared_start && (p & 3) != 0;
+    }
+    __device__ __forceinline__ void put_word(uint32_t wi, uint32_t v) {
+        if (merge_first) {
+            atomicOr(&w[wi], v);
+            merge_first = false;
+        } else {
+            w[wi] = v;
+        }
+    }
+    __device__ __forceinline__ void byte(uint32_t b) {
+        cur |= (b & 0xffu) << (8 * (pos & 3));
+        pos++;
+        if ((pos & 3) == 0) {
+            put_word((pos >> 2) - 1, cur);
+            cur = 0;
+        }
+    }
+    __device__ __forceinline__ void be32(uint32_t v) {
+        const uint32_t le = __byte_perm(v, 0, 0x0123);  // the 4 bytes in memory order
+        const uint32_t off = pos & 3;
+        if (off == 0) {
+            put_word(pos >> 2, le);
+        } else {
+            put_word(pos >> 2, cur | (le << (8 * off)));
+            cur = le >> (32 - 8 * off);
+        }
+        pos += 4;
+    }
+    // pending bytes of a partial last word: merged if the word is shared with the next
+    // record, stored otherwise (the rest of the word belongs to this record)
+    __device__ __forceinline__ void end(bool shared) {
+        if (pos & 3) {
+            if (shared || merge_first)
+                atomicOr(&w[pos >> 2], cur);
+            else
+                w[pos >> 2] = cur;
+        }
+    }
+};
+
+// nb bytes of a k-mer value, big-endian (VKmer bytes after the header)
+template <class K>
+__device__ __forceinline__ void ww_kbytes(WordWriter &o, K v, int nb) {
+    int rem = nb;
+    while (rem >= 4) {
+        o.be32((uint32_t)(v >> (8 * (rem - 4))));
+        rem -= 4;
+    }
+    while (rem > 0) {
+        rem--;
+        o.byte((uint32_t)(v >> (8 * rem)));
+    }
+}
+
+// The same record fields with per-byte window checks, merging every byte with atomicOr
+// (records that straddle two windows).
+struct OrSink {
+    uint32_t *w;
+    long long lo, hi;
+    __device__ __forceinline__ void b(long long pos, uint32_t v) const {
+        if (pos >= lo && pos < hi) {
+            const uint32_t q = (uint32_t)(pos - lo);
+            atomicOr(&w[q >> 2], (v & 0xffu) << (8 * (q & 3)));
+        }
+    }
+    __device__ __forceinline__ void u32(long long pos, uint32_t v) const {
+        b(pos, v >> 24);
+        b(pos + 1, v >> 16);
+        b(pos + 2, v >> 8);
+        b(pos + 3, v);
+    }
+};
+
+template <class K>
+__device__ __forceinline__ void node_neighbors(K key, uint32_t m, int t, int k, K y[4], int &ny) {
+    ny = 0;
+    for (int e = 0; e < 4; e++)
+        if (m & (1u << e)) y[ny++] = edge_neighbor<K>(key, t, e, k);
+    for (int u = 1; u < ny; u++)
+        for (int v = u; v > 0 && y[v] < y[v - 1]; v--) {
+            const K tmp = y[v];
+            y[v] = y[v - 1];
+            y[v - 1] = tmp;
+        }
+}
+
+template <class K>
+__global__ void __launch_bounds__(WRITER_WARPS * 32, 3) k_emit_write_part(EmitArgs a) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint8_t *stage = smem_raw + (size_t)warp * (WARP_STAGE + 32);
+    uint32_t *stage32 = reinterpret_cast<uint32_t *>(stage);
+    const uint32_t p = blockIdx.x;
+    const int k = a.k, nb = (k + 3) / 4;
+    const uint32_t n = a.part_nodes[p];
+    const unsigned long long pbytes = a.part_bytes[p];
+    const unsigned long long base = a.part_off[p];
+    const uint32_t hb = a.head_off[p], hc = a.head_cnt2[p];
+    const unsigned long long nbase = a.node_base[p];
+    const K *nkey = (const K *)a.nkey + nbase;
+    const unsigned long long *ncm = a.ncm + nbase;
+    const uint32_t *noff = a.noff + nbase;
+    const HeadOut *hout = a.hout + hb;
+    const uint32_t npw = (n + WRITER_WARPS - 1) / WRITER_WARPS;
+    const uint32_t j0 = min(n, warp * npw), j1 = min(n, j0 + npw);
+    if (j0 >= j1) return;
+    const unsigned long long wlo = noff[j0];
+    const unsigned long long whi = j1 < n ? (unsigned long long)noff[j1] : pbytes;
+    // this warp's heads: those positioned inside [wlo, whi) (sorted by position)
+    uint32_t hlo = 0, hhi = 0;
+    for (uint32_t i0 = 0; i0 < hc; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const unsigned long long hp = i < hc ? (unsigned long long)hout[i].pos : ~0ULL;
+        hlo += __popc(__ballot_sync(0xffffffffu, i < hc && hp < wlo));
+        hhi += __popc(__ballot_sync(0xffffffffu, i < hc && hp < whi));
+    }
+    const uint32_t iters = (j1 - j0 + 31) / 32;
+    for (unsigned long long W = wlo; W < whi; W += WARP_STAGE) {
+        const unsigned long long wend = min(whi, W + WARP_STAGE);
+        for (uint32_t it = 0; it < iters; it++) {
+            const uint32_t j = j0 + lane + 32 * it;
+            long long st = -1, en = 0;
+            K key = 0;
+            unsigned long long cm = 0;
+            if (j < j1) {
+                st = noff[j];
+                en = j + 1 < n ? (long long)noff[j + 1] : (long long)pbytes;
+                key = nkey[j];
+                cm = ncm[j];
+            }
+            const bool live = st >= 0 && st < (long long)wend && en > (long long)W;
+            const bool whole = live && st >= (long long)W && en <= (long long)wend;
+            // Zero the words merged with atomicOr.  A record zeroes its trailing word (shared
+            // with its successor, written in this or a later iteration), the record opening
+            // the window zeroes word 0, a record crossing a window edge zeroes the words it
+            // owns alone.  A record never zeroes a first word that holds a predecessor's bytes.
+            if (live) {
+                const long long fw = (max(st, (long long)W) - (long long)W) >> 2;
+                const long long lw = (min(en, (long long)wend) - 1 - (long long)W) >> 2;
+                // (a record crossing the window end with <= 4 bytes inside has lw == fw,
+                //  which may already hold its predecessor's bytes)
+                const bool shared_first = st > (long long)W && ((st - (long long)W) & 3) != 0;
+                if (!(lw == fw && shared_first)) stage32[lw] = 0;
+                if (st <= (long long)W) stage32[0] = 0;
+                if (!whole) {
+                    if (((st - (long long)W) & 3) == 0) stage32[fw] = 0;  // not shared when aligned
+                    for (long long q2 = fw + 1; q2 < lw; q2++) stage32[q2] = 0;
+                }
+            }
+            __syncwarp();
+            if (live) {
+                const uint32_t meta = (uint32_t)(cm >> 32);
+                uint32_t active = 0x80u;
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                    if ((meta >> (4 * t)) & 15u) active |= 1u << t;
+                if (meta & META_UNFLIPPED) active |= 0x10u;
+                if (meta & META_FLIPPED) active |= 0x20u;
+                const uint32_t cov = __float_as_uint((float)(uint32_t)cm);
+                if (whole) {
+                    // whole record in the window: word stores
+                    const uint32_t rs = (uint32_t)(st - (long long)W), re = (uint32_t)(en - (long long)W);
+                    WordWriter o;
+                    o.begin(stage32, rs, true);
+                    o.be32((uint32_t)(en - st - 8));
+                    o.be32((uint32_t)(4 + nb));
+                    o.be32((uint32_t)k);
+                    ww_kbytes<K>(o, key, nb);
+                    o.byte(active);
+                    for (int t = 0; t < 4; t++) {
+                        const uint32_t m = (meta >> (4 * t)) & 15u;
+                        if (!m) continue;
+                        const int ny = __popc(m);
+                        o.be32((uint32_t)ny);
+                        if (ny == 1) {
+                            o.be32((uint32_t)k);
+                            ww_kbytes<K>(o, edge_neighbor<K>(key, t, __ffs(m) - 1, k), nb);
+                        } else {
+                            K y[4];
+                            int c;
+                            node_neighbors<K>(key, m, t, k, y, c);
+                            for (int u = 0; u < c; u++) {
+                                o.be32((uint32_t)k);
+                                ww_kbytes<K>(o, y[u], nb);
+                            }
+                        }
+                    }
+                    if (o.pos != re - 4) {  // read-head sets follow (written below)
+                        o.end(false);
+                        o.begin(stage32, re - 4, false);
+                    }
+                    o.be32(cov);
+                    o.end(true);
+                } else {
+                    // record across a window edge: byte by byte
+                    const OrSink o{stage32, (long long)W, (long long)wend};
+                    o.u32(st, (uint32_t)(en - st - 8));
+                    o.u32(st + 4, (uint32_t)(4 + nb));
+                    o.u32(st + 8, (uint32_t)k);
+                    long long pos = st + 12;
+                    for (int i = 0; i < nb; i++) o.b(pos + i, KeyOps<K>::byte_at(key, nb - 1 - i));
+                    pos += nb;
+                    o.b(pos++, active);
+                    for (int t = 0; t < 4; t++) {
+                        const uint32_t m = (meta >> (4 * t)) & 15u;
+                        if (!m) continue;
+                        K y[4];
+                        int ny;
+                        node_neighbors<K>(key, m, t, k, y, ny);
+                        o.u32(pos, (uint32_t)ny);
+                        pos += 4;
+                        for (int u = 0; u < ny; u++) {
+                            o.u32(pos, (uint32_t)k);
+                            pos += 4;
+                            for (int i = 0; i < nb; i++) o.b(pos + i, KeyOps<K>::byte_at(y[u], nb - 1 - i));
+                            pos += nb;
+                        }
+                    }
+                    o.u32(en - 4, cov);
+                }
+            }
+            __syncwarp();
+        }
+        // read heads: set header, flags, uuid, lengths, packed letters
+        const Sink ow{stage, (long long)W, (long long)wend, false};
+        for (uint32_t h = hlo; h < hhi; h++) {
+            const HeadOut ho = hout[h];
+            const uint32_t nbr = packed_len(ho.L), nbm = packed_len(ho.Lm);
+            const long long hp = ho.pos;
+            const long long hsz = 13 + nbr + (ho.Lm ? 4 + nbm : 0);
+            if (!ow.touches(hp - (ho.set_count ? 5 : 0), hsz + 5)) continue;
+            if (lane == 0) {
+                if (ho.set_count) {
+                    ow.b(hp - 5, 1);  // ExternalableTreeSet: whole body in stream
+                    ow.u32(hp - 4, ho.set_count);
+                }
+                ow.b(hp, ho.Lm ? 1u : 0u);
+                ow.u32(hp + 1, (uint32_t)(ho.uuid >> 32));
+                ow.u32(hp + 5, (uint32_t)ho.uuid);
+                ow.u32(hp + 9, ho.L);
+                if (ho.Lm) ow.u32(hp + 13 + nbr, ho.Lm);
+            }
+            pack_seq_warp(ow, hp + 13, a.text + ho.s_off, ho.L, lane);
+            if (ho.Lm) pack_seq_warp(ow, hp + 17 + nbr, a.text + ho.m_off, ho.Lm, lane);
+        }
+        __syncwarp();
+        // window out with aligned 16-byte stores
+        const unsigned long long g0 = base + W, g1 = base + wend;
+        for (unsigned long long c = (g0 & ~15ULL) + 16ULL * lane; c < g1; c += 16ULL * 32) {
+            if (c >= g0 && c + 16 <= g1) {
+                const uint32_t ofs = (uint32_t)(c - g0);
+                const uint32_t w0 = ofs >> 2, sh = (ofs & 3u) * 8u;
+                uint32_t w[5];
+#pragma unroll
+                for (int q = 0; q < 5; q++) w[q] = stage32[w0 + q];
+                uint4 v;
+                v.x = __funnelshift_r(w[0], w[1], sh);
+                v.y = __funnelshift_r(w[1], w[2], sh);
+                v.z = __funnelshift_r(w[2], w[3], sh);
+                v.w = __funnelshift_r(w[3], w[4], sh);
+                *reinterpret_cast<uint4 *>(a.out + c) = v;
+            } else {
+                for (int q = 0; q < 16; q++) {
+                    const unsigned long long g = c + q;
+                    if (g >= g0 && g < g1) a.out[g] = stage[g - g0];
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+void launch_emit_write_part(const EmitArgs &a, cudaStream_t s) {
+    if (!a.g.nparts) return;
+    const size_t sm = (size_t)WRITER_WARPS * (WARP_STAGE + 32);
+    t_launches++;
+    if (a.g.wide) {
+        cudaFuncSetAttribute(k_emit_write_part<u128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_emit_write_part<u128><<<a.g.nparts, WRITER_WARPS * 32, sm, s>>>(a);
+    } else {
+        cudaFuncSetAttribute(k_emit_write_part<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_emit_write_part<uint64_t><<<a.g.nparts, WRITER_WARPS * 32, sm, s>>>(a);
     }
 }
 

@@ -71,8 +71,75 @@ struct EmitArgs {
     const unsigned long long *part_off;
     uint8_t *out;
     DevStatus *st;
+    // partitioned build: compacted nodes of partition p at node_base[p] in nkey / ncm
+    const void *nkey = nullptr;
+    const unsigned long long *ncm = nullptr;
+    const unsigned long long *node_base = nullptr;
+    const uint32_t *noff = nullptr;
+    const HeadOut *hout = nullptr;
 };
 void launch_emit_prepare(const EmitArgs &a, cudaStream_t s);
 void launch_emit_write(const EmitArgs &a, cudaStream_t s);
+
+// ---- partitioned build --------------------------------------------------------------------
+// Occurrences are streamed into S super buckets (top hash bits), each super bucket into F
+// fine buckets; a fine bucket's distinct k-mers are aggregated in a shared-memory table.
+constexpr int HLL_REGS = 2048;               // HyperLogLog registers for the distinct estimate
+constexpr uint32_t AGG_SLOTS = 2048;         // shared-memory table of one fine bucket
+constexpr uint32_t AGG_TARGET = 896;         // distinct k-mers per fine bucket aimed for
+constexpr uint32_t CHUNK = 4096;             // occurrences per CTA in the fine passes
+constexpr int SC_THREADS = 256;              // super scatter: one read per thread
+constexpr int SC_ROUND = 16;                 // k-mers per thread per staging round
+constexpr uint32_t MAX_SUPERS = 2048, MAX_FINE = 2048;
+
+struct PartPlan {
+    uint32_t log_s;  // S = 1 << log_s super buckets
+    uint32_t F;      // fine buckets per super bucket
+    uint32_t P;      // S * F
+};
+// distinct k-mer estimate from the HyperLogLog registers
+double hll_estimate(const uint32_t *regs);
+PartPlan plan_partitions(double distinct_est, double safety, double target);
+
+void launch_count_occ(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines, const uint32_t *reads,
+                      const uint32_t *n_reads_dev, uint32_t n_reads_max, int k, uint32_t log_s, uint32_t *s_cnt,
+                      uint32_t *hll, cudaStream_t s);
+void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
+                          const uint32_t *reads, uint32_t n_reads, int k, uint32_t log_s, const unsigned long long *s_off, uint32_t *s_cur,
+                          void *okey, uint16_t *obits, cudaStream_t s);
+// chunks: (start, super << 32 | length) of CHUNK-sized pieces of each super bucket
+void launch_fine_count(int wide, const void *okey, const ulonglong2 *chunks, uint32_t n_chunks, PartPlan pp,
+                       unsigned long long *fine_cnt, cudaStream_t s);
+void launch_scatter_fine(int wide, const void *okey, const uint16_t *obits, const ulonglong2 *chunks,
+                         uint32_t n_chunks, PartPlan pp, const unsigned long long *fine_off, uint32_t *fine_cur,
+                         void *okey2, uint16_t *obits2, cudaStream_t s);
+void launch_heads_part(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines, const uint32_t *reads,
+                       uint32_t n_reads, int k, PartPlan pp, Head *heads, uint32_t *head_cnt, cudaStream_t s);
+struct AggArgs {
+    int wide;
+    int k;
+    PartPlan pp;
+    const void *okey2;
+    const uint16_t *obits2;
+    const unsigned long long *fine_off;
+    const LineRec *lines;
+    const uint32_t *reads;
+    Head *heads;
+    uint32_t *head_idx;
+    unsigned long long *head_sk;
+    const uint32_t *head_off;
+    const uint32_t *head_cnt;
+    uint32_t *head_cnt2;
+    void *nkey;                 // node keys (written over okey2)
+    unsigned long long *ncm;    // count | meta << 32
+    uint32_t *noff;             // partition-local byte offset of each node's record
+    HeadOut *hout;              // read heads in output order (indexed like head_idx)
+    uint32_t *part_nodes;
+    unsigned long long *part_bytes;
+    DevStatus *st;
+};
+void launch_aggregate(const AggArgs &a, cudaStream_t s);
+// record writer of the partitioned build (node offsets and head positions precomputed)
+void launch_emit_write_part(const EmitArgs &a, cudaStream_t s);
 
 }  // namespace gx

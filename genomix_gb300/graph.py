@@ -131,12 +131,14 @@ class GraphBuildJob:
     """One graph build: inputs -> run() -> (VKmer, Node) records."""
 
     def __init__(self, ctx, kmer_length, input_kind="readid", paired=False, out_parts=1, load_factor=0.0,
-                 max_readids_per_edge=250, threads_per_read=0, est_input_bytes=0):
+                 max_readids_per_edge=250, threads_per_read=0, est_input_bytes=0, algorithm="partitioned"):
         self.ctx = ctx
         self._L = ctx._L
         kind = {"readid": _lib.INPUT_READID, "fastq": _lib.INPUT_FASTQ}[input_kind]
+        algo = {"default": _lib.ALGO_DEFAULT, "partitioned": _lib.ALGO_PARTITIONED, "table": _lib.ALGO_TABLE}[algorithm]
         o = _lib.JobOpts(ctypes.sizeof(_lib.JobOpts), int(kmer_length), kind, 1 if paired else 0, int(out_parts),
-                         float(load_factor), int(max_readids_per_edge), int(threads_per_read), int(est_input_bytes))
+                         float(load_factor), int(max_readids_per_edge), int(threads_per_read), int(est_input_bytes),
+                         algo)
         h = ctypes.c_void_p()
         _check(self._L.gx_job_create(ctx.h, ctypes.byref(o), ctypes.byref(h)), "gx_job_create")
         self.h = h.value

@@ -85,11 +85,21 @@ typedef struct gx_job_opts {
     int input_kind;           /* GX_INPUT_READID or GX_INPUT_FASTQ */
     int paired;               /* FASTQ only: 1 = mate streams 0 and 1 are paired files */
     int out_parts;            /* output parts (SequenceFile part files); 0 means 1 */
-    double load_factor;       /* table slots = occurrences / load_factor; 0 = default (0.5) */
+    double load_factor;       /* fill of the hash tables aimed for; 0 = default (table build: slots =
+                                 occurrences / 0.5; partitioned build: 896 of 2048 per bucket) */
     int max_readids_per_edge; /* accepted and ignored, as in the reference (GenomixJobConf.java:718) */
     int threads_per_read;     /* 0 = autotuned; 1 = thread per read; 32 = warp per read */
     size_t est_input_bytes;   /* capacity hint for the device input buffer; 0 = grow on demand */
+    int algorithm;            /* GX_ALGO_*: how occurrences are aggregated */
 } gx_job_opts;
+
+/* Aggregation algorithms (gx_job_opts.algorithm); both give identical records. */
+enum {
+    GX_ALGO_DEFAULT = 0,      /* the partitioned build */
+    GX_ALGO_PARTITIONED = 1,  /* stream occurrences into hash buckets, aggregate each bucket in
+                                 shared memory (no random DRAM access) */
+    GX_ALGO_TABLE = 2         /* one open-addressing table in HBM, CAS inserts per occurrence */
+};
 
 typedef struct gx_stats {
     uint64_t lines;           /* input lines (readid) or records (FASTQ) */
