@@ -2007,6 +2007,64 @@ struct WordWriter {
     }
 };
 
+// Bytes appended in memory order to a shared window through a 64-bit accumulator: one
+// word store per 4 bytes.  The first word is merged with atomicOr when the record starts
+// mid-word (it holds the predecessor's last bytes); finish() merges the trailing partial
+// word when it is shared with the next record.
+struct ByteAcc {
+    uint32_t *w;
+    uint32_t wi;       // word the accumulator fills
+    uint32_t first;    // record's first word
+    uint32_t fill;     // bytes in acc
+    bool merge_first;
+    unsigned long long acc;
+    __device__ __forceinline__ void init(uint32_t *w_, uint32_t pos, bool shared_start) {
+        w = w_;
+        wi = pos >> 2;
+        first = wi;
+        fill = pos & 3;
+        merge_first = shared_start && fill != 0;
+        acc = 0;
+    }
+    __device__ __forceinline__ void store(uint32_t v) {
+        if (merge_first && wi == first)
+            atomicOr(&w[wi], v);
+        else
+            w[wi] = v;
+    }
+    // n <= 4 bytes, the first in the low byte of le
+    __device__ __forceinline__ void put(uint32_t le, uint32_t n) {
+        acc |= (unsigned long long)le << (8 * fill);
+        fill += n;
+        if (fill >= 4) {
+            store((uint32_t)acc);
+            wi++;
+            acc >>= 32;
+            fill -= 4;
+        }
+    }
+    __device__ __forceinline__ void be32(uint32_t v) { put(__byte_perm(v, 0, 0x0123), 4); }
+    __device__ __forceinline__ void byte(uint32_t b) { put(b & 0xffu, 1); }
+    __device__ __forceinline__ void finish(bool shared_end) {
+        if (fill) {
+            if (shared_end || (merge_first && wi == first))
+                atomicOr(&w[wi], (uint32_t)acc);
+            else
+                w[wi] = (uint32_t)acc;
+        }
+    }
+};
+
+// nb bytes of a k-mer value, big-endian, in groups of up to 4
+template <class K>
+__device__ __forceinline__ void acc_kbytes(ByteAcc &o, K v, int nb) {
+    for (int rem = nb; rem > 0; rem -= 4) {
+        const int n = rem < 4 ? rem : 4;
+        const uint32_t chunk = (uint32_t)(v >> (8 * (rem - n))) << (8 * (4 - n));  // BE bytes at the top
+        o.put(__byte_perm(chunk, 0, 0x0123), (uint32_t)n);
+    }
+}
+
 // nb bytes of a k-mer value, big-endian (VKmer bytes after the header)
 template <class K>
 __device__ __forceinline__ void ww_kbytes(WordWriter &o, K v, int nb) {
@@ -2051,6 +2109,74 @@ __device__ __forceinline__ void node_neighbors(K key, uint32_t m, int t, int k, 
             y[v] = y[v - 1];
             y[v - 1] = tmp;
         }
+}
+
+// a record that crosses a window edge: byte by byte, merged with atomicOr (rare)
+template <class K>
+__device__ __forceinline__ void write_record_straddling(uint32_t *stage32, long long W, long long wend, long long st,
+                                                     long long en, K key, uint32_t meta, uint32_t active, uint32_t cov,
+                                                     int k, int nb) {
+    const OrSink o{stage32, W, wend};
+    o.u32(st, (uint32_t)(en - st - 8));
+    o.u32(st + 4, (uint32_t)(4 + nb));
+    o.u32(st + 8, (uint32_t)k);
+    long long pos = st + 12;
+    for (int i = 0; i < nb; i++) o.b(pos + i, KeyOps<K>::byte_at(key, nb - 1 - i));
+    pos += nb;
+    o.b(pos++, active);
+    for (int t = 0; t < 4; t++) {
+        const uint32_t m = (meta >> (4 * t)) & 15u;
+        if (!m) continue;
+        K y[4];
+        int ny;
+        node_neighbors<K>(key, m, t, k, y, ny);
+        o.u32(pos, (uint32_t)ny);
+        pos += 4;
+        for (int u = 0; u < ny; u++) {
+            o.u32(pos, (uint32_t)k);
+            pos += 4;
+            for (int i = 0; i < nb; i++) o.b(pos + i, KeyOps<K>::byte_at(y[u], nb - 1 - i));
+            pos += nb;
+        }
+    }
+    o.u32(en - 4, cov);
+}
+
+// a list with 2..4 neighbours (a branching node), sorted ascending
+template <class K>
+__device__ __forceinline__ void acc_branch_list(ByteAcc &o, K key, uint32_t m, int t, int k, int nb) {
+    K y[4];
+    int c;
+    node_neighbors<K>(key, m, t, k, y, c);
+    for (int u = 0; u < c; u++) {
+        o.be32((uint32_t)k);
+        acc_kbytes<K>(o, y[u], nb);
+    }
+}
+
+// the read-head sets of the warp's heads inside the window
+__device__ __forceinline__ void write_heads_window(const Sink &ow, const HeadOut *hout, uint32_t hlo, uint32_t hhi,
+                                                const uint8_t *text, int lane) {
+    for (uint32_t h = hlo; h < hhi; h++) {
+        const HeadOut ho = hout[h];
+        const uint32_t nbr = packed_len(ho.L), nbm = packed_len(ho.Lm);
+        const long long hp = ho.pos;
+        const long long hsz = 13 + nbr + (ho.Lm ? 4 + nbm : 0);
+        if (!ow.touches(hp - (ho.set_count ? 5 : 0), hsz + 5)) continue;
+        if (lane == 0) {
+            if (ho.set_count) {
+                ow.b(hp - 5, 1);  // ExternalableTreeSet: whole body in stream
+                ow.u32(hp - 4, ho.set_count);
+            }
+            ow.b(hp, ho.Lm ? 1u : 0u);
+            ow.u32(hp + 1, (uint32_t)(ho.uuid >> 32));
+            ow.u32(hp + 5, (uint32_t)ho.uuid);
+            ow.u32(hp + 9, ho.L);
+            if (ho.Lm) ow.u32(hp + 13 + nbr, ho.Lm);
+        }
+        pack_seq_warp(ow, hp + 13, text + ho.s_off, ho.L, lane);
+        if (ho.Lm) pack_seq_warp(ow, hp + 17 + nbr, text + ho.m_off, ho.Lm, lane);
+    }
 }
 
 template <class K>
@@ -2129,89 +2255,44 @@ __global__ void __launch_bounds__(WRITER_WARPS * 32, 3) k_emit_write_part(EmitAr
                 if (whole) {
                     // whole record in the window: word stores
                     const uint32_t rs = (uint32_t)(st - (long long)W), re = (uint32_t)(en - (long long)W);
-                    WordWriter o;
-                    o.begin(stage32, rs, true);
+                    ByteAcc o;
+                    o.init(stage32, rs, true);
                     o.be32((uint32_t)(en - st - 8));
                     o.be32((uint32_t)(4 + nb));
                     o.be32((uint32_t)k);
-                    ww_kbytes<K>(o, key, nb);
+                    acc_kbytes<K>(o, key, nb);
                     o.byte(active);
-                    for (int t = 0; t < 4; t++) {
+                    // present edge lists, walked uniformly: one list per step
+                    uint32_t lists = active & 15u;
+                    const uint32_t nl = __popc(lists);
+                    for (uint32_t li = 0; li < nl; li++) {
+                        const int t = __ffs(lists) - 1;
+                        lists &= lists - 1;
                         const uint32_t m = (meta >> (4 * t)) & 15u;
-                        if (!m) continue;
                         const int ny = __popc(m);
                         o.be32((uint32_t)ny);
                         if (ny == 1) {
                             o.be32((uint32_t)k);
-                            ww_kbytes<K>(o, edge_neighbor<K>(key, t, __ffs(m) - 1, k), nb);
+                            acc_kbytes<K>(o, edge_neighbor<K>(key, t, __ffs(m) - 1, k), nb);
                         } else {
-                            K y[4];
-                            int c;
-                            node_neighbors<K>(key, m, t, k, y, c);
-                            for (int u = 0; u < c; u++) {
-                                o.be32((uint32_t)k);
-                                ww_kbytes<K>(o, y[u], nb);
-                            }
+                            acc_branch_list<K>(o, key, m, t, k, nb);
                         }
                     }
-                    if (o.pos != re - 4) {  // read-head sets follow (written below)
-                        o.end(false);
-                        o.begin(stage32, re - 4, false);
+                    if ((o.wi << 2) + o.fill != re - 4) {  // read-head sets follow (written below)
+                        o.finish(false);
+                        o.init(stage32, re - 4, false);
                     }
                     o.be32(cov);
-                    o.end(true);
+                    o.finish(true);
                 } else {
-                    // record across a window edge: byte by byte
-                    const OrSink o{stage32, (long long)W, (long long)wend};
-                    o.u32(st, (uint32_t)(en - st - 8));
-                    o.u32(st + 4, (uint32_t)(4 + nb));
-                    o.u32(st + 8, (uint32_t)k);
-                    long long pos = st + 12;
-                    for (int i = 0; i < nb; i++) o.b(pos + i, KeyOps<K>::byte_at(key, nb - 1 - i));
-                    pos += nb;
-                    o.b(pos++, active);
-                    for (int t = 0; t < 4; t++) {
-                        const uint32_t m = (meta >> (4 * t)) & 15u;
-                        if (!m) continue;
-                        K y[4];
-                        int ny;
-                        node_neighbors<K>(key, m, t, k, y, ny);
-                        o.u32(pos, (uint32_t)ny);
-                        pos += 4;
-                        for (int u = 0; u < ny; u++) {
-                            o.u32(pos, (uint32_t)k);
-                            pos += 4;
-                            for (int i = 0; i < nb; i++) o.b(pos + i, KeyOps<K>::byte_at(y[u], nb - 1 - i));
-                            pos += nb;
-                        }
-                    }
-                    o.u32(en - 4, cov);
+                    write_record_straddling<K>(stage32, (long long)W, (long long)wend, st, en, key, meta, active, cov, k,
+                                               nb);
                 }
             }
             __syncwarp();
         }
         // read heads: set header, flags, uuid, lengths, packed letters
-        const Sink ow{stage, (long long)W, (long long)wend, false};
-        for (uint32_t h = hlo; h < hhi; h++) {
-            const HeadOut ho = hout[h];
-            const uint32_t nbr = packed_len(ho.L), nbm = packed_len(ho.Lm);
-            const long long hp = ho.pos;
-            const long long hsz = 13 + nbr + (ho.Lm ? 4 + nbm : 0);
-            if (!ow.touches(hp - (ho.set_count ? 5 : 0), hsz + 5)) continue;
-            if (lane == 0) {
-                if (ho.set_count) {
-                    ow.b(hp - 5, 1);  // ExternalableTreeSet: whole body in stream
-                    ow.u32(hp - 4, ho.set_count);
-                }
-                ow.b(hp, ho.Lm ? 1u : 0u);
-                ow.u32(hp + 1, (uint32_t)(ho.uuid >> 32));
-                ow.u32(hp + 5, (uint32_t)ho.uuid);
-                ow.u32(hp + 9, ho.L);
-                if (ho.Lm) ow.u32(hp + 13 + nbr, ho.Lm);
-            }
-            pack_seq_warp(ow, hp + 13, a.text + ho.s_off, ho.L, lane);
-            if (ho.Lm) pack_seq_warp(ow, hp + 17 + nbr, a.text + ho.m_off, ho.Lm, lane);
-        }
+        if (hlo < hhi) write_heads_window(Sink{stage, (long long)W, (long long)wend, false}, hout, hlo, hhi, a.text, lane);
         __syncwarp();
         // window out with aligned 16-byte stores
         const unsigned long long g0 = base + W, g1 = base + wend;
