@@ -24,7 +24,7 @@ EXPORTS = [
     "gx_job_create", "gx_job_add_input", "gx_job_add_input_device", "gx_job_run", "gx_job_emit",
     "gx_job_emit_rewind", "gx_job_records_device", "gx_job_stats", "gx_job_destroy", "gx_batch_run", "gx_pinned_alloc",
     "gx_pinned_free", "gx_fastq_to_readid", "gx_host_free", "gx_seqfile_write", "gx_seqfile_read",
-    "gx_records_to_text",
+    "gx_records_to_text", "gx_build_noalloc",
 ]
 
 
@@ -99,6 +99,7 @@ def load():
         "gx_seqfile_write": ([vp, sz, vp, ctypes.c_uint64, P(vp), P(sz)], i),
         "gx_seqfile_read": ([vp, sz, P(vp), P(sz)], i),
         "gx_records_to_text": ([vp, sz, P(vp), P(sz)], i),
+        "gx_build_noalloc": ([i, vp, sz, i, vp, sz, P(sz)], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

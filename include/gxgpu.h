@@ -186,6 +186,32 @@ void gx_job_destroy(gx_job *job);
  * statuses[i] (may be NULL); the call returns the first non-OK status. */
 gx_status gx_batch_run(gx_ctx *ctx, gx_job **jobs, int n, gx_status *statuses);
 
+/* ---- graph build without device allocation ------------------------------------------- */
+
+/* Bytes of the device scratch array behind gx_build_noalloc. */
+#define GX_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* Graph build of one small readid input, for callers that cannot allocate device memory:
+ * a JVM or service that manages its own slice of device memory and forbids allocations
+ * behind its back, or a process whose device allocator is exhausted or locked.  The call
+ * makes no cudaMalloc, cudaFree or other allocating call; all working memory comes from a
+ * file-scope device array of GX_NOALLOC_SCRATCH_BYTES, which every GPU that loads this
+ * library holds until the process exits.  The caller passes the readid text (device memory,
+ * 16-byte aligned) and a device output buffer (16-byte aligned, out_cap bytes) that
+ * receives the same record stream gx_job_run writes with algorithm GX_ALGO_TABLE.
+ *  - The first call on a device looks up the array's device address with that device
+ *    current; make that first call before any stream capture.
+ *  - Work runs on the legacy default stream of `device`; the call returns when it is done.
+ *  - Calls share the one array (each starts by clearing what must start at zero): calls
+ *    that overlap on the GPU, from different host threads, race and must not be made.
+ *  - An input whose working set does not fit the array returns GX_ENOMEM with a message
+ *    on stderr (about 800,000 k-mer occurrences fit for k <= 32, half that above).
+ *    An output buffer that is too small (or NULL) returns GX_EINVAL with *out_bytes set
+ *    to the size needed; the next call with a larger buffer repeats the whole build.
+ * No counterpart in the reference: its graph build always runs on the JVM heap. */
+gx_status gx_build_noalloc(int device, const void *text_dev, size_t n_text, int k, void *out_dev, size_t out_cap,
+                           size_t *out_bytes);
+
 /* ---- host helpers -------------------------------------------------------------------- */
 
 /* Page-locked host memory, suitable for direct ByteBuffers / FFM MemorySegments. */

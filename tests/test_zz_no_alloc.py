@@ -1,0 +1,82 @@
+"""gx_build_noalloc (the graph build inside the library's fixed device scratch array) against
+gx_job_run with the table algorithm on the same input, through the C ABI.
+
+The file name sorts last so that the entry point is also exercised after every other GPU test
+has run in the same process (device state, the caching allocator and the scratch array's
+leftovers from earlier calls).
+"""
+import ctypes
+
+import pytest
+
+import genomix_gb300 as gx
+from genomix_gb300 import _lib, synth
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+GX_EINVAL, GX_ENOMEM = 1, 6  # gx_status values from include/gxgpu.h
+
+
+def job_records(text, k):
+    with gx.Context(0) as ctx:
+        job = gx.GraphBuildJob(ctx, k, algorithm="table")
+        job.add_input(text)
+        job.run()
+        rec = job.records()
+        st = job.stats()
+        job.close()
+    return rec, st
+
+
+def noalloc(L, text_dev, n_text, k, out_dev, cap):
+    need = ctypes.c_size_t(0)
+    st = L.gx_build_noalloc(0, text_dev, n_text, k, out_dev, cap, ctypes.byref(need))
+    return st, need.value
+
+
+@pytest.mark.parametrize("k", [21, 55])
+def test_noalloc_matches_job_run_twice(k):
+    L = _lib.load()
+    w = synth.plain_cpu(max_reads=4000)
+    text = w.text
+    ref, st = job_records(text, k)
+    assert st["nodes"] > 0 and len(ref) > 0
+    t = torch.frombuffer(bytearray(text), dtype=torch.uint8).cuda()
+    cap = len(ref) + 4096
+    outs = []
+    for _ in range(2):  # two calls in a row reuse the same scratch array
+        out = torch.full((cap,), 0xAB, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        status, n = noalloc(L, t.data_ptr(), t.numel(), k, out.data_ptr(), cap)
+        assert status == _lib.GX_OK, _lib.status_str(status)
+        assert n == len(ref)
+        got = out[:n].cpu().numpy().tobytes()
+        assert got == ref
+        assert bool((out[n:] == 0xAB).all())  # nothing written past the records
+        outs.append(got)
+    assert outs[0] == outs[1]
+
+
+def test_noalloc_size_query_and_limits():
+    L = _lib.load()
+    k = 31
+    text = synth.plain_cpu(max_reads=2000).text
+    ref, _ = job_records(text, k)
+    t = torch.frombuffer(bytearray(text), dtype=torch.uint8).cuda()
+    # no output buffer: the size needed comes back with GX_EINVAL
+    status, need = noalloc(L, t.data_ptr(), t.numel(), k, None, 0)
+    assert status == GX_EINVAL and need == len(ref)
+    # an input far beyond the scratch array is refused cleanly ...
+    big = torch.frombuffer(bytearray(synth.plain_cpu().text * 4), dtype=torch.uint8).cuda()
+    out = torch.empty(1 << 20, dtype=torch.uint8, device="cuda")
+    status, _ = noalloc(L, big.data_ptr(), big.numel(), k, out.data_ptr(), out.numel())
+    assert status == GX_ENOMEM
+    # ... and the next call still gives the reference records
+    out = torch.empty(need, dtype=torch.uint8, device="cuda")
+    status, n = noalloc(L, t.data_ptr(), t.numel(), k, out.data_ptr(), need)
+    assert status == _lib.GX_OK and out[:n].cpu().numpy().tobytes() == ref
+    # empty input: nothing to do
+    status, n = noalloc(L, t.data_ptr(), 0, k, out.data_ptr(), need)
+    assert status == _lib.GX_OK and n == 0
