@@ -13,8 +13,11 @@ reads, see genomix_gb300/synth.py).
              flush is needed between steps)
   e2e        the same metric through the C ABI with host buffers: pinned readid text in,
              H2D copy, build, D2H copy of every record into pinned memory, per step
-  roofline   the table-insert kernel (k_insert): 64 B per k-mer occurrence (one 32 B sector
-             read + one written back) against the measured HBM copy bandwidth
+  roofline   the dominant kernel of the build, the record writer (k_emit_write_part, about
+             40% of the device time): its algorithmic bytes per launch (the record stream
+             written, plus the compacted nodes and read heads it reads) over its CUDA-event
+             duration, against the measured HBM copy bandwidth; `random_access` gives
+             k-mers/s against the hash-table random-access bound (64 B per occurrence)
   cpu_baseline  the oracle (C++ restatement of the reference's sort + group graph build) on
              the first pairs of the same workload, all host threads
 
@@ -37,7 +40,8 @@ METRIC = "k-mers/s, bit-exact graph build, batched vs per-job, 1 GB300; p99 job 
 UNIT = "k-mers/s"
 CPU_SAMPLE_PAIRS = 120_000   # cpu_baseline sample (one run)
 REF_STEP_PAIRS = 60_000      # --impl reference: sample per step
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_insert_pe5mbp_ncu.txt")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_emit_write_part_pe5mbp_k31.md")
+HEADOUT_BYTES = 48           # one HeadOut entry (uuid, two text offsets, position, counts)
 
 
 def peaks():
@@ -49,17 +53,27 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(kmers):
-    """DRAM bytes per k_insert launch from the committed ncu summary, scaled to this launch's
-    occurrences (the capture runs a smaller case; traffic grows with the occurrences)."""
+def profiled_traffic(alg_bytes):
+    """DRAM bytes per record-writer launch from the committed ncu summary: the capture runs a
+    smaller case of the same workload, whose DRAM bytes per algorithmic byte scale to this
+    launch (the writer's traffic grows in proportion to the records it writes)."""
     if not os.path.exists(PROFILE_TRAFFIC):
         return None
-    per_occ = None
+    ratio = None
     with open(PROFILE_TRAFFIC) as f:
         for line in f:
-            if line.startswith("dram_bytes_per_occurrence:"):
-                per_occ = float(line.split(":")[1])
-    return None if per_occ is None else per_occ * kmers
+            if line.startswith("dram_bytes_per_algorithmic_byte:"):
+                ratio = float(line.split(":")[1])
+    return None if ratio is None else ratio * alg_bytes
+
+
+def writer_alg_bytes(st, k, read_len, paired):
+    """Bytes the record writer must move per launch: the records it writes, the compacted node
+    arrays it reads (key, count/meta word, node offset) and, per read head, its HeadOut entry
+    and the letters of the read and its mate."""
+    kb = 8 if k <= 32 else 16
+    letters = read_len * (2 if paired else 1)
+    return st["record_bytes"] + st["nodes"] * (kb + 8 + 4) + st["read_heads"] * (HEADOUT_BYTES + letters)
 
 
 class ClockSampler:
@@ -255,8 +269,10 @@ def run_gb300(args, ws, rank, local):
         return
     peak, peak_kind = peaks()
     ins_ms = statistics.mean(s["ms_insert"] for s in stats)
-    achieved = 64.0 * kmers / (ins_ms / 1e3) / 1e9
-    traffic = profiled_traffic(kmers)
+    wr_ms = statistics.mean(s["ms_write"] for s in stats)
+    wr_bytes = writer_alg_bytes(stats[0], w.k, 150, True)
+    achieved = wr_bytes / (wr_ms / 1e3) / 1e9
+    traffic = profiled_traffic(wr_bytes)
     b_alg = len(w.text) + 64.0 * kmers + out_bytes
     job_ms = ms / args.steps
     cb = None
@@ -271,13 +287,17 @@ def run_gb300(args, ws, rank, local):
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": len(w.text),
                 "d2h_bytes_per_step": out_bytes, "ms_per_step": ms_e2e / args.steps},
-        "roofline": {"bound": "hbm", "kernel": "k_insert", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth",
-                     "traffic": traffic, "alg_bytes_per_unit": 64, "units_per_launch": kmers},
+        "roofline": {"bound": "hbm", "kernel": "k_emit_write_part", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth",
+                     "traffic": traffic, "alg_bytes_per_launch": wr_bytes, "ms_per_launch": wr_ms,
+                     "unit_of_work": "record byte written (plus its node and read-head inputs)"},
+        "random_access": {"bound_kmers_per_s": peak * 1e9 / 64.0, "frac": value / ws / (peak * 1e9 / 64.0),
+                          "note": "64 B per k-mer occurrence (one 32 B sector read + one written)"},
         "job_roofline": {"alg_bytes": b_alg, "achieved_gbs": b_alg / (job_ms / 1e3) / 1e9,
                          "frac": b_alg / (job_ms / 1e3) / 1e9 / peak},
-        "phases_ms": {"parse": statistics.mean(s["ms_parse"] for s in stats), "insert": ins_ms,
-                      "emit": statistics.mean(s["ms_emit"] for s in stats), "job": job_ms},
+        "phases_ms": {"parse": statistics.mean(s["ms_parse"] for s in stats), "partition": ins_ms,
+                      "aggregate": statistics.mean(s["ms_aggregate"] for s in stats), "write": wr_ms,
+                      "job": job_ms},
         "graph": {"kmers": kmers, "reads": stats[0]["reads"], "nodes": stats[0]["nodes"],
                   "read_heads": stats[0]["read_heads"], "record_bytes": out_bytes,
                   "table_slots": stats[0]["table_slots"], "max_probe": stats[0]["max_probe"]},

@@ -55,7 +55,7 @@ class Stats(ctypes.Structure):
         ("cov_inexact_nodes", ctypes.c_uint64), ("max_probe", ctypes.c_uint32), ("key_bits", ctypes.c_uint32),
         ("kernel_launches", ctypes.c_uint64),
         ("ms_parse", ctypes.c_double), ("ms_insert", ctypes.c_double), ("ms_emit", ctypes.c_double),
-        ("ms_total", ctypes.c_double),
+        ("ms_total", ctypes.c_double), ("ms_aggregate", ctypes.c_double), ("ms_write", ctypes.c_double),
     ]
 
     def as_dict(self):

@@ -591,6 +591,8 @@ static gx_status build_table(RunCtx &rc) {
         j->st.cov_inexact_nodes = hs.cov_inexact;
         j->st.ms_insert = tm.ms(2, 3);
         j->st.ms_emit = tm.ms(3, 4) + tm.ms(5, 6);
+        j->st.ms_aggregate = tm.ms(3, 4);
+        j->st.ms_write = tm.ms(5, 6);
         j->st.ms_total = tm.ms(0, 6);
         return GX_OK;
     }
@@ -782,6 +784,8 @@ static gx_status build_partitioned(RunCtx &rc) {
         j->st.cov_inexact_nodes = hs.cov_inexact;
         j->st.ms_insert = tm.ms(2, 3);
         j->st.ms_emit = tm.ms(3, 4) + tm.ms(5, 6);
+        j->st.ms_aggregate = tm.ms(3, 4);
+        j->st.ms_write = tm.ms(5, 6);
         j->st.ms_total = tm.ms(0, 6);
         return GX_OK;
     }

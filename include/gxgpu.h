@@ -119,6 +119,8 @@ typedef struct gx_stats {
     double ms_insert;         /* device time of k-mer extraction + table inserts */
     double ms_emit;           /* device time of compaction + record serialization */
     double ms_total;          /* device time of gx_job_run */
+    double ms_aggregate;      /* device time of the per-bucket aggregation (part of ms_emit) */
+    double ms_write;          /* device time of the record-writer kernel (part of ms_emit) */
 } gx_stats;
 
 /* ---- context ------------------------------------------------------------------------- */
