@@ -18,102 +18,12 @@
 
 #include "../../include/gxgpu.h"
 #include "gx_host.h"
+#include "gx_job_internal.h"
 #include "gx_kernels.cuh"
 
 using namespace gx;
 
-namespace {
-
-enum JobState { JS_INPUT = 0, JS_RAN = 1, JS_FAILED = 2 };
-
-struct Timers {
-    cudaEvent_t ev[10] = {};
-    bool ok = false;
-    void init() {
-        for (auto &e : ev)
-            if (cudaEventCreate(&e) != cudaSuccess) return;
-        ok = true;
-    }
-    void destroy() {
-        for (auto &e : ev)
-            if (e) cudaEventDestroy(e);
-    }
-    float ms(int a, int b) const {
-        float t = 0;
-        if (ok) cudaEventElapsedTime(&t, ev[a], ev[b]);
-        return t;
-    }
-};
-
-}  // namespace
-
-struct gx_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::mutex mu;
-    size_t mem_limit = 0;
-    cudaEvent_t marks[16] = {};
-};
-
-struct gx_job {
-    gx_ctx *ctx = nullptr;
-    gx_job_opts o{};
-    int k = 0;
-    int wide = 0;
-    JobState state = JS_INPUT;
-    // readid input on the device
-    uint8_t *d_text = nullptr;
-    size_t text_len = 0, text_cap = 0;
-    bool text_borrowed = false;
-    int n_device_inputs = 0;
-    // FASTQ inputs kept on the host until run (mate stream 0 / 1, one entry per file)
-    std::vector<std::string> fastq[2];
-    // results
-    uint8_t *d_out = nullptr;
-    size_t out_bytes = 0;
-    uint32_t nparts = 0;
-    unsigned long long *d_part_off = nullptr;  // table-partition byte offsets (nparts + 1)
-    std::vector<uint64_t> part_bounds;         // output-part byte offsets (out_parts + 1)
-    std::vector<uint64_t> cursor;              // emit cursor per output part
-    std::vector<unsigned long long> h_part_off;  // lazily fetched copy of d_part_off
-    gx_stats st{};
-    Timers tm;
-};
-
-#define CK(call)                                                                                    \
-    do {                                                                                            \
-        cudaError_t e_ = (call);                                                                    \
-        if (e_ != cudaSuccess) {                                                                    \
-            fprintf(stderr, "gxgpu: %s failed: %s (%s:%d)\n", #call, cudaGetErrorString(e_), __FILE__, \
-                    __LINE__);                                                                      \
-            return e_ == cudaErrorMemoryAllocation ? GX_ENOMEM : GX_ECUDA;                          \
-        }                                                                                           \
-    } while (0)
-
-// Allocations of one run, released together (stream ordered).
-struct RunArena {
-    cudaStream_t s;
-    std::vector<void *> ptrs;
-    explicit RunArena(cudaStream_t st) : s(st) {}
-    template <class T>
-    gx_status alloc(T *&p, size_t count) {
-        void *q = nullptr;
-        const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
-        cudaError_t e = cudaMallocAsync(&q, bytes, s);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return GX_ENOMEM;
-        }
-        ptrs.push_back(q);
-        p = (T *)q;
-        return GX_OK;
-    }
-    void release() {
-        for (void *p : ptrs) cudaFreeAsync(p, s);
-        ptrs.clear();
-    }
-    ~RunArena() { release(); }
-};
+using namespace gxi;
 
 static gx_status ensure_text_cap(gx_job *j, size_t need) {
     if (j->text_borrowed) {
@@ -310,22 +220,12 @@ gx_status gx_job_add_input_device(gx_job *j, const void *dev, size_t bytes, int 
     return append_text(j, dev, bytes, cudaMemcpyDeviceToDevice, last == '\n');
 }
 
-static gx_status run_job(gx_job *j);
-
 gx_status gx_job_run(gx_job *j) {
     if (!j) return GX_EINVAL;
     if (j->state != JS_INPUT) return GX_ESTATE;
     std::lock_guard<std::mutex> lk(j->ctx->mu);
     cudaSetDevice(j->ctx->device);
-    const uint64_t l0 = launches_this_thread();
-    gx_status st = run_job(j);
-    j->st.kernel_launches = launches_this_thread() - l0;
-    j->state = st == GX_OK ? JS_RAN : JS_FAILED;
-    if (j->text_borrowed) {
-        j->d_text = nullptr;  // the caller's buffer is no longer referenced
-        j->text_borrowed = false;
-    }
-    return st;
+    return run_job_locked(j);
 }
 
 gx_status gx_job_stats(const gx_job *j, gx_stats *out) {
@@ -409,23 +309,15 @@ void gx_job_destroy(gx_job *j) {
         cudaSetDevice(j->ctx->device);
         cudaStream_t s = j->ctx->stream;
         if (j->d_text && !j->text_borrowed) cudaFreeAsync(j->d_text, s);
-        if (j->d_out) cudaFreeAsync(j->d_out, s);
+        if (j->out_owner)
+            j->out_owner.reset();  // the last job of a batch frees the shared record buffer
+        else if (j->d_out)
+            cudaFreeAsync(j->d_out, s);
         if (j->d_part_off) cudaFreeAsync(j->d_part_off, s);
         cudaStreamSynchronize(s);
         j->tm.destroy();
     }
     delete j;
-}
-
-gx_status gx_batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses) {
-    if (!c || (!jobs && n) || n < 0) return GX_EINVAL;
-    gx_status first = GX_OK;
-    for (int i = 0; i < n; i++) {
-        gx_status s = jobs[i] && jobs[i]->ctx == c ? gx_job_run(jobs[i]) : GX_EINVAL;
-        if (statuses) statuses[i] = s;
-        if (s != GX_OK && first == GX_OK) first = s;
-    }
-    return first;
 }
 
 }  // extern "C"
@@ -667,6 +559,23 @@ static gx_status build_partitioned(RunCtx &rc) {
         if ((e = tar.alloc(part_bytes, P)) != GX_OK) return e;
         void *pscratch;
         if ((e = tar.alloc(pscratch, scan_scratch_bytes(P + 1, 8))) != GX_OK) return e;
+        // the job is a batch of one sample
+        SamplePlan *d_plan;
+        SuperInfo *d_sinfo;
+        uint32_t *d_rbase;
+        if ((e = tar.alloc(d_plan, 1)) != GX_OK) return e;
+        if ((e = tar.alloc(d_sinfo, S)) != GX_OK) return e;
+        if ((e = tar.alloc(d_rbase, 2)) != GX_OK) return e;
+        {
+            const SamplePlan hp{0, pp.log_s, pp.F, 0};
+            std::vector<SuperInfo> hsi(S);
+            for (uint32_t q = 0; q < S; q++) hsi[q] = SuperInfo{q * pp.F, pp.F, pp.log_s, 0};
+            const uint32_t hrb[2] = {0, n_reads};
+            CK(cudaMemcpyAsync(d_plan, &hp, sizeof hp, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(d_sinfo, hsi.data(), S * sizeof(SuperInfo), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(d_rbase, hrb, sizeof hrb, cudaMemcpyHostToDevice, s));
+        }
+        const SampleMap smap{d_rbase, d_plan, 1};
         void *part_off_v = nullptr;
         CK(cudaMallocAsync(&part_off_v, (P + 1) * sizeof(unsigned long long), s));
         part_off = (unsigned long long *)part_off_v;
@@ -680,14 +589,15 @@ static gx_status build_partitioned(RunCtx &rc) {
         CK(cudaMemsetAsync(head_cur, 0, P * 4ull, s));
         CK(cudaEventRecord(tm.ev[2], s));
         // A2, read heads
-        launch_scatter_super(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, pp.log_s, d_soff, s_cur, okey, obits, s);
-        launch_heads_part(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, pp, heads, head_cnt, s);
+        launch_scatter_super(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, S, d_soff, s_cur, okey,
+                             obits, s);
+        launch_heads_part(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, heads, head_cnt, s);
         exclusive_scan_u32(head_cnt, head_off, P, nullptr, pscratch, s);
         launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, P, s);
         // B1, B2
-        launch_fine_count(wide, okey, d_chunks, n_chunks, pp, fine_cnt, s);
+        launch_fine_count(wide, okey, d_chunks, n_chunks, d_sinfo, fine_cnt, s);
         exclusive_scan_u64(fine_cnt, fine_off, P, fine_off + P, pscratch, s);
-        launch_scatter_fine(wide, okey, obits, d_chunks, n_chunks, pp, fine_off, fine_cur, okey2, obits2, s);
+        launch_scatter_fine(wide, okey, obits, d_chunks, n_chunks, d_sinfo, fine_off, fine_cur, okey2, obits2, s);
         CK(cudaEventRecord(tm.ev[3], s));
         // C
         AggArgs g{};
@@ -791,14 +701,10 @@ static gx_status build_partitioned(RunCtx &rc) {
     }
 }
 
-static gx_status run_job(gx_job *j) {
-    cudaStream_t s = j->ctx->stream;
-    Timers &tm = j->tm;
-    memset(&j->st, 0, sizeof j->st);
-    j->st.key_bits = j->wide ? 128 : 64;
-    const int k = j->k;
-    const bool partitioned = j->o.algorithm != GX_ALGO_TABLE;
+namespace gxi {
 
+gx_status prepare_text(gx_job *j) {
+    cudaStream_t s = j->ctx->stream;
     // FASTQ: the reference driver's conversion, then the readid path
     if (j->o.input_kind == GX_INPUT_FASTQ) {
         const size_t nf = j->fastq[0].size();
@@ -816,6 +722,22 @@ static gx_status run_job(gx_job *j) {
         }
         j->fastq[0].clear();
         j->fastq[1].clear();
+    }
+    return GX_OK;
+}
+
+}  // namespace gxi
+
+static gx_status run_job(gx_job *j) {
+    cudaStream_t s = j->ctx->stream;
+    Timers &tm = j->tm;
+    memset(&j->st, 0, sizeof j->st);
+    j->st.key_bits = j->wide ? 128 : 64;
+    const int k = j->k;
+    const bool partitioned = j->o.algorithm != GX_ALGO_TABLE;
+    {
+        const gx_status pe = prepare_text(j);
+        if (pe != GX_OK) return pe;
     }
 
     const uint64_t n_text = j->text_len;
@@ -900,4 +822,16 @@ static gx_status run_job(gx_job *j) {
     rc.n_reads = n_reads;
     rc.n_occ = hs.n_occ;
     return partitioned ? build_partitioned(rc) : build_table(rc);
+}
+
+gx_status gxi::run_job_locked(gx_job *j) {
+    const uint64_t l0 = launches_this_thread();
+    gx_status st = run_job(j);
+    j->st.kernel_launches = launches_this_thread() - l0;
+    j->state = st == GX_OK ? JS_RAN : JS_FAILED;
+    if (j->text_borrowed) {
+        j->d_text = nullptr;  // the caller's buffer is no longer referenced
+        j->text_borrowed = false;
+    }
+    return st;
 }

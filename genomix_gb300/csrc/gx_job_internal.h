@@ -1,0 +1,116 @@
+// gx_job_internal.h — contexts, jobs and run-scoped device memory, shared by the plain build
+// (gx_job.cu) and the batched and served builds (gx_batch.cu, gx_serve.cu).
+#pragma once
+#include <algorithm>
+#include <cstdio>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gxgpu.h"
+#include "gx_kernels.cuh"
+
+namespace gxi {
+
+enum JobState { JS_INPUT = 0, JS_RAN = 1, JS_FAILED = 2 };
+
+struct Timers {
+    cudaEvent_t ev[10] = {};
+    bool ok = false;
+    void init() {
+        for (auto &e : ev)
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+        ok = true;
+    }
+    void destroy() {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    float ms(int a, int b) const {
+        float t = 0;
+        if (ok) cudaEventElapsedTime(&t, ev[a], ev[b]);
+        return t;
+    }
+};
+
+}  // namespace gxi
+
+struct gx_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    size_t mem_limit = 0;
+    cudaEvent_t marks[16] = {};
+};
+
+struct gx_job {
+    gx_ctx *ctx = nullptr;
+    gx_job_opts o{};
+    int k = 0;
+    int wide = 0;
+    gxi::JobState state = gxi::JS_INPUT;
+    // readid input on the device
+    uint8_t *d_text = nullptr;
+    size_t text_len = 0, text_cap = 0;
+    bool text_borrowed = false;
+    int n_device_inputs = 0;
+    // FASTQ inputs kept on the host until run (mate stream 0 / 1, one entry per file)
+    std::vector<std::string> fastq[2];
+    // results
+    uint8_t *d_out = nullptr;
+    size_t out_bytes = 0;
+    uint32_t nparts = 0;
+    unsigned long long *d_part_off = nullptr;  // table-partition byte offsets (nparts + 1)
+    std::vector<uint64_t> part_bounds;         // output-part byte offsets (out_parts + 1)
+    std::vector<uint64_t> cursor;              // emit cursor per output part
+    std::vector<unsigned long long> h_part_off;  // lazily fetched copy of d_part_off
+    gx_stats st{};
+    gxi::Timers tm;
+    // a batched run writes every sample's records into one buffer: the jobs share ownership
+    std::shared_ptr<void> out_owner;
+};
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            fprintf(stderr, "gxgpu: %s failed: %s (%s:%d)\n", #call, cudaGetErrorString(e_), __FILE__, \
+                    __LINE__);                                                                      \
+            return e_ == cudaErrorMemoryAllocation ? GX_ENOMEM : GX_ECUDA;                          \
+        }                                                                                           \
+    } while (0)
+
+namespace gxi {
+
+// Allocations of one run, released together (stream ordered).
+struct RunArena {
+    cudaStream_t s;
+    std::vector<void *> ptrs;
+    explicit RunArena(cudaStream_t st) : s(st) {}
+    template <class T>
+    gx_status alloc(T *&p, size_t count) {
+        void *q = nullptr;
+        const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+        cudaError_t e = cudaMallocAsync(&q, bytes, s);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return GX_ENOMEM;
+        }
+        ptrs.push_back(q);
+        p = (T *)q;
+        return GX_OK;
+    }
+    void release() {
+        for (void *p : ptrs) cudaFreeAsync(p, s);
+        ptrs.clear();
+    }
+    ~RunArena() { release(); }
+};
+
+// Runs one job; the caller holds the context's lock and has made its device current.
+gx_status run_job_locked(gx_job *j);
+// FASTQ inputs converted to readid text on the device (the reference driver's pre-pass).
+gx_status prepare_text(gx_job *j);
+
+}  // namespace gxi

@@ -1280,10 +1280,28 @@ __device__ __forceinline__ void walker_for(Walker<K> &w, const uint8_t *text, un
 }
 
 __device__ __forceinline__ uint32_t super_of(uint64_t h, uint32_t log_s) { return (uint32_t)(h >> (64 - log_s)); }
-// fine bucket (global index) of a key hash; the 32 hash bits below the super bits pick
-// the fine bucket inside the super bucket; the low bits are left for the table slot
-__device__ __forceinline__ uint32_t fine_of(uint64_t h, const PartPlan &pp) {
-    return super_of(h, pp.log_s) * pp.F + __umulhi((uint32_t)(h >> (32 - pp.log_s)), pp.F);
+
+// super bucket inside a sample (log_s may be 0) and fine bucket inside a super bucket: the
+// 32 hash bits below the super bits pick the fine bucket; the low bits are left for the
+// shared-memory table slot
+__device__ __forceinline__ uint32_t super_local(uint64_t h, uint32_t log_s) {
+    return log_s ? (uint32_t)(h >> (64 - log_s)) : 0u;
+}
+__device__ __forceinline__ uint32_t fine_in_super(uint64_t h, uint32_t log_s, uint32_t F) {
+    return __umulhi((uint32_t)(h >> (32 - log_s)), F);
+}
+// sample owning read r: the last s with read_base[s] <= r (empty samples are skipped)
+__device__ __forceinline__ uint32_t sample_of_read(const SampleMap &m, uint32_t r) {
+    if (m.n <= 1) return 0;
+    uint32_t lo = 0, hi = m.n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&m.read_base[mid]) <= r)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
 }
 
 // Exclusive scan, in place, of a shared array of n <= blockDim * 32 entries; returns the total.
@@ -1383,6 +1401,97 @@ void launch_count_occ(int wide, const uint8_t *text, uint64_t n_text, const Line
                                                      hll);
 }
 
+// Batched A1.  Each CTA takes a contiguous range of reads and walks it one sample segment at a
+// time, with the segment's super histogram and HyperLogLog registers in shared memory.
+template <class K>
+__global__ void __launch_bounds__(256) k_count_occ_batch(const uint8_t *text, unsigned long long n_text,
+                                                         const LineRec *lines, const uint32_t *reads,
+                                                         const uint32_t *read_base, uint32_t n_samples, int k,
+                                                         uint32_t *s_cnt, uint32_t *hll) {
+    __shared__ uint32_t hist[MAX_SUPERS];
+    __shared__ uint32_t reg[HLL_REGS];
+    const uint32_t n_reads = read_base[n_samples];
+    uint32_t r0 = (uint32_t)((unsigned long long)blockIdx.x * n_reads / gridDim.x);
+    const uint32_t r1 = (uint32_t)((unsigned long long)(blockIdx.x + 1) * n_reads / gridDim.x);
+    SampleMap m{read_base, nullptr, n_samples};
+    uint32_t smp = r0 < r1 ? sample_of_read(m, r0) : n_samples;
+    while (r0 < r1) {
+        const uint32_t seg_end = min(r1, read_base[smp + 1]);
+        for (uint32_t i = threadIdx.x; i < MAX_SUPERS; i += blockDim.x) hist[i] = 0;
+        for (uint32_t i = threadIdx.x; i < HLL_REGS; i += blockDim.x) reg[i] = 0;
+        __syncthreads();
+        for (uint32_t r = r0 + threadIdx.x; r < seg_end; r += blockDim.x) {
+            Walker<K> w;
+            walker_for(w, text, n_text, lines, reads, r, k);
+            while (!w.done()) {
+                K c;
+                uint32_t b, d;
+                w.next(c, b, d);
+                const uint64_t h = KeyOps<K>::hash(c);
+                atomicAdd(&hist[(uint32_t)(h >> 53)], 1u);
+                const uint64_t w2 = h >> 11;
+                const uint32_t rho = w2 ? (uint32_t)(__clzll(w2) - 10) : 54u;
+                atomicMax(&reg[h & (HLL_REGS - 1)], rho);
+            }
+        }
+        __syncthreads();
+        uint32_t *gc = s_cnt + (size_t)smp * MAX_SUPERS, *gh = hll + (size_t)smp * HLL_REGS;
+        for (uint32_t i = threadIdx.x; i < MAX_SUPERS; i += blockDim.x)
+            if (hist[i]) atomicAdd(&gc[i], hist[i]);
+        for (uint32_t i = threadIdx.x; i < HLL_REGS; i += blockDim.x)
+            if (reg[i]) atomicMax(&gh[i], reg[i]);
+        __syncthreads();
+        r0 = seg_end;
+        smp++;
+        while (smp < n_samples && read_base[smp + 1] <= r0) smp++;  // skip empty samples
+    }
+}
+
+void launch_count_occ_batch(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
+                            const uint32_t *reads, const uint32_t *read_base, uint32_t n_samples,
+                            uint32_t n_reads_max, int k, uint32_t *s_cnt, uint32_t *hll, cudaStream_t s) {
+    if (!n_reads_max || !n_samples) return;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((n_reads_max + 255) / 256, 152ull * 8);
+    t_launches++;
+    if (wide)
+        k_count_occ_batch<u128><<<blocks, 256, 0, s>>>(text, n_text, lines, reads, read_base, n_samples, k, s_cnt,
+                                                       hll);
+    else
+        k_count_occ_batch<uint64_t><<<blocks, 256, 0, s>>>(text, n_text, lines, reads, read_base, n_samples, k,
+                                                           s_cnt, hll);
+}
+
+__global__ void k_sample_bounds(const unsigned long long *text_base, uint32_t n_samples,
+                                const unsigned long long *line_end, uint32_t n_lines, const uint32_t *nvalid,
+                                const uint32_t *nvalid_total, uint32_t *line_base, uint32_t *read_base) {
+    const uint32_t smp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (smp > n_samples) return;
+    uint32_t lb = n_lines;
+    if (smp < n_samples) {
+        // first line whose terminator lies at or after the sample's first byte
+        const unsigned long long tb = text_base[smp];
+        uint32_t lo = 0, hi = n_lines;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (line_end[mid] < tb)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        lb = lo;
+    }
+    line_base[smp] = lb;
+    read_base[smp] = lb < n_lines ? nvalid[lb] : *nvalid_total;
+}
+
+void launch_sample_bounds(const unsigned long long *text_base, uint32_t n_samples,
+                          const unsigned long long *line_end, uint32_t n_lines, const uint32_t *nvalid,
+                          const uint32_t *nvalid_total, uint32_t *line_base, uint32_t *read_base, cudaStream_t s) {
+    t_launches++;
+    k_sample_bounds<<<(n_samples + 1 + 127) / 128, 128, 0, s>>>(text_base, n_samples, line_end, n_lines, nvalid,
+                                                                nvalid_total, line_base, read_base);
+}
+
 // ---- A2 -------------------------------------------------------------------------------------
 // shared layout of k_scatter_super: staging for one round, then three S-entry arrays
 template <class K>
@@ -1400,18 +1509,23 @@ template <class K>
 __global__ void __launch_bounds__(SC_THREADS) k_scatter_super(const uint8_t *text, unsigned long long n_text,
                                                               const LineRec *lines,
                                                               const uint32_t *reads, uint32_t n_reads, int k,
-                                                              uint32_t log_s, const unsigned long long *s_off,
+                                                              SampleMap m, uint32_t S,
+                                                              const unsigned long long *s_off,
                                                               uint32_t *s_cur, K *okey, uint16_t *obits) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     SuperSmem<K> &sm = *reinterpret_cast<SuperSmem<K> *>(smem_raw);
-    const uint32_t S = 1u << log_s;
     uint32_t *const sm_loff = sm.arrays, *const sm_gbase = sm.arrays + S, *const sm_cur = sm.arrays + 2 * S;
     const uint32_t r = blockIdx.x * SC_THREADS + threadIdx.x;
     Walker<K> w;
-    if (r < n_reads)
+    uint32_t sbase = 0, log_s = 0;
+    if (r < n_reads) {
         walker_for(w, text, n_text, lines, reads, r, k);
-    else
+        const SamplePlan pl = m.plan[sample_of_read(m, r)];
+        sbase = pl.super_base;
+        log_s = pl.log_s;
+    } else {
         w.empty();
+    }
     if (threadIdx.x == 0) sm.rounds = 0;
     __syncthreads();
     atomicMax(&sm.rounds, (w.nk + SC_ROUND - 1) / SC_ROUND);
@@ -1426,7 +1540,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_scatter_super(const uint8_t *tex
             K c;
             uint32_t b, d;
             w.next(c, b, d);
-            atomicAdd(&sm_cur[super_of(KeyOps<K>::hash(c), log_s)], 1u);
+            atomicAdd(&sm_cur[sbase + super_local(KeyOps<K>::hash(c), log_s)], 1u);
         }
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) {
@@ -1443,7 +1557,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_scatter_super(const uint8_t *tex
             K c;
             uint32_t b, d;
             w.next(c, b, d);
-            const uint32_t sp = super_of(KeyOps<K>::hash(c), log_s);
+            const uint32_t sp = sbase + super_local(KeyOps<K>::hash(c), log_s);
             const uint32_t pos = sm_loff[sp] + atomicAdd(&sm_cur[sp], 1u);
             sm.key[pos] = c;
             sm.bits[pos] = (uint16_t)b;
@@ -1462,49 +1576,50 @@ __global__ void __launch_bounds__(SC_THREADS) k_scatter_super(const uint8_t *tex
 }
 
 void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
-                          const uint32_t *reads, uint32_t n_reads, int k, uint32_t log_s, const unsigned long long *s_off, uint32_t *s_cur,
-                          void *okey, uint16_t *obits, cudaStream_t s) {
+                          const uint32_t *reads, uint32_t n_reads, int k, SampleMap m, uint32_t n_super,
+                          const unsigned long long *s_off, uint32_t *s_cur, void *okey, uint16_t *obits,
+                          cudaStream_t s) {
     if (!n_reads) return;
     const unsigned blocks = (n_reads + SC_THREADS - 1) / SC_THREADS;
     t_launches++;
     if (wide) {
-        const size_t sm = SuperSmem<u128>::bytes(1u << log_s);
+        const size_t sm = SuperSmem<u128>::bytes(n_super);
         cudaFuncSetAttribute(k_scatter_super<u128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_scatter_super<u128><<<blocks, SC_THREADS, sm, s>>>(text, n_text, lines, reads, n_reads, k, log_s, s_off,
-                                                             s_cur, (u128 *)okey, obits);
+        k_scatter_super<u128><<<blocks, SC_THREADS, sm, s>>>(text, n_text, lines, reads, n_reads, k, m, n_super,
+                                                             s_off, s_cur, (u128 *)okey, obits);
     } else {
-        const size_t sm = SuperSmem<uint64_t>::bytes(1u << log_s);
+        const size_t sm = SuperSmem<uint64_t>::bytes(n_super);
         cudaFuncSetAttribute(k_scatter_super<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_scatter_super<uint64_t><<<blocks, SC_THREADS, sm, s>>>(text, n_text, lines, reads, n_reads, k, log_s,
-                                                                 s_off, s_cur, (uint64_t *)okey, obits);
+        k_scatter_super<uint64_t><<<blocks, SC_THREADS, sm, s>>>(text, n_text, lines, reads, n_reads, k, m,
+                                                                 n_super, s_off, s_cur, (uint64_t *)okey, obits);
     }
 }
 
 // ---- B1 -------------------------------------------------------------------------------------
 template <class K>
-__global__ void __launch_bounds__(256) k_fine_count(const K *okey, const ulonglong2 *chunks, PartPlan pp,
+__global__ void __launch_bounds__(256) k_fine_count(const K *okey, const ulonglong2 *chunks, const SuperInfo *sinfo,
                                                     unsigned long long *fine_cnt) {
     __shared__ uint32_t bins[MAX_FINE];
     const ulonglong2 ch = chunks[blockIdx.x];
     const uint32_t sp = (uint32_t)(ch.y >> 32), len = (uint32_t)ch.y;
-    for (uint32_t i = threadIdx.x; i < pp.F; i += blockDim.x) bins[i] = 0;
+    const SuperInfo si = sinfo[sp];
+    for (uint32_t i = threadIdx.x; i < si.F; i += blockDim.x) bins[i] = 0;
     __syncthreads();
-    const uint32_t f0 = sp * pp.F;
     for (uint32_t i = threadIdx.x; i < len; i += blockDim.x)
-        atomicAdd(&bins[fine_of(KeyOps<K>::hash(okey[ch.x + i]), pp) - f0], 1u);
+        atomicAdd(&bins[fine_in_super(KeyOps<K>::hash(okey[ch.x + i]), si.log_s, si.F)], 1u);
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < pp.F; i += blockDim.x)
-        if (bins[i]) atomicAdd(&fine_cnt[f0 + i], (unsigned long long)bins[i]);
+    for (uint32_t i = threadIdx.x; i < si.F; i += blockDim.x)
+        if (bins[i]) atomicAdd(&fine_cnt[si.fine_first + i], (unsigned long long)bins[i]);
 }
 
-void launch_fine_count(int wide, const void *okey, const ulonglong2 *chunks, uint32_t n_chunks, PartPlan pp,
-                       unsigned long long *fine_cnt, cudaStream_t s) {
+void launch_fine_count(int wide, const void *okey, const ulonglong2 *chunks, uint32_t n_chunks,
+                       const SuperInfo *sinfo, unsigned long long *fine_cnt, cudaStream_t s) {
     if (!n_chunks) return;
     t_launches++;
     if (wide)
-        k_fine_count<u128><<<n_chunks, 256, 0, s>>>((const u128 *)okey, chunks, pp, fine_cnt);
+        k_fine_count<u128><<<n_chunks, 256, 0, s>>>((const u128 *)okey, chunks, sinfo, fine_cnt);
     else
-        k_fine_count<uint64_t><<<n_chunks, 256, 0, s>>>((const uint64_t *)okey, chunks, pp, fine_cnt);
+        k_fine_count<uint64_t><<<n_chunks, 256, 0, s>>>((const uint64_t *)okey, chunks, sinfo, fine_cnt);
 }
 
 // ---- B2 -------------------------------------------------------------------------------------
@@ -1520,17 +1635,18 @@ struct FineSmem {
 
 template <class K>
 __global__ void __launch_bounds__(256) k_scatter_fine(const K *okey, const uint16_t *obits, const ulonglong2 *chunks,
-                                                      PartPlan pp, const unsigned long long *fine_off,
+                                                      const SuperInfo *sinfo, const unsigned long long *fine_off,
                                                       uint32_t *fine_cur, K *okey2, uint16_t *obits2) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     FineSmem<K> &sm = *reinterpret_cast<FineSmem<K> *>(smem_raw);
     const ulonglong2 ch = chunks[blockIdx.x];
     const uint32_t sp = (uint32_t)(ch.y >> 32), len = (uint32_t)ch.y;
-    const uint32_t f0 = sp * pp.F, F = pp.F;
+    const SuperInfo si = sinfo[sp];
+    const uint32_t f0 = si.fine_first, F = si.F, log_s = si.log_s;
     for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) sm.cur[i] = 0;
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < len; i += blockDim.x)
-        atomicAdd(&sm.cur[fine_of(KeyOps<K>::hash(okey[ch.x + i]), pp) - f0], 1u);
+        atomicAdd(&sm.cur[fine_in_super(KeyOps<K>::hash(okey[ch.x + i]), log_s, F)], 1u);
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) {
         sm.loff[i] = sm.cur[i];
@@ -1542,7 +1658,7 @@ __global__ void __launch_bounds__(256) k_scatter_fine(const K *okey, const uint1
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
         const K key = okey[ch.x + i];
-        const uint32_t b = fine_of(KeyOps<K>::hash(key), pp) - f0;
+        const uint32_t b = fine_in_super(KeyOps<K>::hash(key), log_s, F);
         const uint32_t pos = sm.loff[b] + atomicAdd(&sm.cur[b], 1u);
         sm.key[pos] = key;
         sm.bits[pos] = obits[ch.x + i];
@@ -1550,7 +1666,7 @@ __global__ void __launch_bounds__(256) k_scatter_fine(const K *okey, const uint1
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
         const K key = sm.key[i];
-        const uint32_t b = fine_of(KeyOps<K>::hash(key), pp) - f0;
+        const uint32_t b = fine_in_super(KeyOps<K>::hash(key), log_s, F);
         const unsigned long long g = fine_off[f0 + b] + sm.gbase[b] + (i - sm.loff[b]);
         okey2[g] = key;
         obits2[g] = sm.bits[i];
@@ -1558,19 +1674,19 @@ __global__ void __launch_bounds__(256) k_scatter_fine(const K *okey, const uint1
 }
 
 void launch_scatter_fine(int wide, const void *okey, const uint16_t *obits, const ulonglong2 *chunks,
-                         uint32_t n_chunks, PartPlan pp, const unsigned long long *fine_off, uint32_t *fine_cur,
-                         void *okey2, uint16_t *obits2, cudaStream_t s) {
+                         uint32_t n_chunks, const SuperInfo *sinfo, const unsigned long long *fine_off,
+                         uint32_t *fine_cur, void *okey2, uint16_t *obits2, cudaStream_t s) {
     if (!n_chunks) return;
     t_launches++;
     if (wide) {
         const size_t sm = sizeof(FineSmem<u128>);
         cudaFuncSetAttribute(k_scatter_fine<u128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_scatter_fine<u128><<<n_chunks, 256, sm, s>>>((const u128 *)okey, obits, chunks, pp, fine_off, fine_cur,
+        k_scatter_fine<u128><<<n_chunks, 256, sm, s>>>((const u128 *)okey, obits, chunks, sinfo, fine_off, fine_cur,
                                                       (u128 *)okey2, obits2);
     } else {
         const size_t sm = sizeof(FineSmem<uint64_t>);
         cudaFuncSetAttribute(k_scatter_fine<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_scatter_fine<uint64_t><<<n_chunks, 256, sm, s>>>((const uint64_t *)okey, obits, chunks, pp, fine_off,
+        k_scatter_fine<uint64_t><<<n_chunks, 256, sm, s>>>((const uint64_t *)okey, obits, chunks, sinfo, fine_off,
                                                           fine_cur, (uint64_t *)okey2, obits2);
     }
 }
@@ -1579,7 +1695,7 @@ void launch_scatter_fine(int wide, const void *okey, const uint16_t *obits, cons
 template <class K>
 __global__ void k_heads_part(const uint8_t *text, unsigned long long n_text, const LineRec *lines,
                              const uint32_t *reads, uint32_t n_reads,
-                             int k, PartPlan pp, Head *heads, uint32_t *head_cnt) {
+                             int k, SampleMap m, Head *heads, uint32_t *head_cnt) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n_reads) return;
     Walker<K> w;
@@ -1589,7 +1705,9 @@ __global__ void k_heads_part(const uint8_t *text, unsigned long long n_text, con
     w.next(c, b, d);
     const uint32_t mate = reads[r] & 1u;
     const long long rid = lines[reads[r] >> 1].read_id;
-    const uint32_t f = fine_of(KeyOps<K>::hash(c), pp);
+    const SamplePlan pl = m.plan[sample_of_read(m, r)];
+    const uint64_t h = KeyOps<K>::hash(c);
+    const uint32_t f = pl.fine_base + super_local(h, pl.log_s) * pl.F + fine_in_super(h, pl.log_s, pl.F);
     Head hd;
     hd.part = f;
     hd.slot = 0;
@@ -1602,14 +1720,14 @@ __global__ void k_heads_part(const uint8_t *text, unsigned long long n_text, con
 }
 
 void launch_heads_part(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines, const uint32_t *reads,
-                       uint32_t n_reads, int k, PartPlan pp, Head *heads, uint32_t *head_cnt, cudaStream_t s) {
+                       uint32_t n_reads, int k, SampleMap m, Head *heads, uint32_t *head_cnt, cudaStream_t s) {
     if (!n_reads) return;
     t_launches++;
     if (wide)
-        k_heads_part<u128><<<(n_reads + 255) / 256, 256, 0, s>>>(text, n_text, lines, reads, n_reads, k, pp, heads,
+        k_heads_part<u128><<<(n_reads + 255) / 256, 256, 0, s>>>(text, n_text, lines, reads, n_reads, k, m, heads,
                                                                 head_cnt);
     else
-        k_heads_part<uint64_t><<<(n_reads + 255) / 256, 256, 0, s>>>(text, n_text, lines, reads, n_reads, k, pp,
+        k_heads_part<uint64_t><<<(n_reads + 255) / 256, 256, 0, s>>>(text, n_text, lines, reads, n_reads, k, m,
                                                                     heads, head_cnt);
 }
 

@@ -101,20 +101,54 @@ struct PartPlan {
 double hll_estimate(const uint32_t *regs);
 PartPlan plan_partitions(double distinct_est, double safety, double target);
 
+// Bucket plan of one sample.  A batch of samples shares one bucket space: sample s owns the
+// super buckets [super_base, super_base + 2^log_s) and the fine buckets
+// [fine_base, fine_base + 2^log_s * F), so its records come out as one contiguous run.  A
+// plain job is a batch of one sample with super_base = fine_base = 0.
+struct SamplePlan {
+    uint32_t super_base;
+    uint32_t log_s;  // 0 allowed: one super bucket
+    uint32_t F;      // fine buckets per super bucket
+    uint32_t fine_base;
+};
+// Per global super bucket: its first global fine bucket, its fine-bucket count and the
+// owning sample's log_s (the hash bits below the super bits pick the fine bucket).
+struct SuperInfo {
+    uint32_t fine_first, F, log_s, pad;
+};
+// Reads of sample s are [read_base[s], read_base[s + 1]).
+struct SampleMap {
+    const uint32_t *read_base;  // n + 1 entries
+    const SamplePlan *plan;     // n entries
+    uint32_t n;
+};
+
 void launch_count_occ(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines, const uint32_t *reads,
                       const uint32_t *n_reads_dev, uint32_t n_reads_max, int k, uint32_t log_s, uint32_t *s_cnt,
                       uint32_t *hll, cudaStream_t s);
+// Batched A1: per sample, MAX_SUPERS super counts (top 11 hash bits) and HLL_REGS
+// HyperLogLog registers, at s_cnt + s * MAX_SUPERS and hll + s * HLL_REGS.
+void launch_count_occ_batch(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
+                            const uint32_t *reads, const uint32_t *read_base, uint32_t n_samples,
+                            uint32_t n_reads_max, int k, uint32_t *s_cnt, uint32_t *hll, cudaStream_t s);
+// read_base[s] for each sample from the text offset where the sample starts: the first line
+// that starts at or after text_base[s] (line_end: exclusive line ends; nvalid: exclusive
+// scan of valid mates per line, total at nvalid_total).
+void launch_sample_bounds(const unsigned long long *text_base, uint32_t n_samples,
+                          const unsigned long long *line_end, uint32_t n_lines, const uint32_t *nvalid,
+                          const uint32_t *nvalid_total, uint32_t *line_base, uint32_t *read_base, cudaStream_t s);
 void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
-                          const uint32_t *reads, uint32_t n_reads, int k, uint32_t log_s, const unsigned long long *s_off, uint32_t *s_cur,
-                          void *okey, uint16_t *obits, cudaStream_t s);
+                          const uint32_t *reads, uint32_t n_reads, int k, SampleMap m, uint32_t n_super,
+                          const unsigned long long *s_off, uint32_t *s_cur, void *okey, uint16_t *obits,
+                          cudaStream_t s);
 // chunks: (start, super << 32 | length) of CHUNK-sized pieces of each super bucket
-void launch_fine_count(int wide, const void *okey, const ulonglong2 *chunks, uint32_t n_chunks, PartPlan pp,
-                       unsigned long long *fine_cnt, cudaStream_t s);
+void launch_fine_count(int wide, const void *okey, const ulonglong2 *chunks, uint32_t n_chunks,
+                       const SuperInfo *sinfo, unsigned long long *fine_cnt, cudaStream_t s);
 void launch_scatter_fine(int wide, const void *okey, const uint16_t *obits, const ulonglong2 *chunks,
-                         uint32_t n_chunks, PartPlan pp, const unsigned long long *fine_off, uint32_t *fine_cur,
-                         void *okey2, uint16_t *obits2, cudaStream_t s);
+                         uint32_t n_chunks, const SuperInfo *sinfo, const unsigned long long *fine_off,
+                         uint32_t *fine_cur, void *okey2, uint16_t *obits2, cudaStream_t s);
 void launch_heads_part(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines, const uint32_t *reads,
-                       uint32_t n_reads, int k, PartPlan pp, Head *heads, uint32_t *head_cnt, cudaStream_t s);
+                       uint32_t n_reads, int k, SampleMap m, Head *heads, uint32_t *head_cnt, cudaStream_t s);
 struct AggArgs {
     int wide;
     int k;

@@ -180,12 +180,18 @@ gx_status gx_job_stats(const gx_job *job, gx_stats *out);
 
 void gx_job_destroy(gx_job *job);
 
-/* ---- batched: many jobs in one persistent launch ------------------------------------- */
+/* ---- batched: many jobs in one pass over the device ---------------------------------- */
 
 /* Run n jobs of one context together.  Every job must have its inputs added and not yet
- * have run.  Each job gets its own table partition range, k and output; the result of
- * every job is identical to its gx_job_run result.  Per-job status codes go to
- * statuses[i] (may be NULL); the call returns the first non-OK status. */
+ * have run.  Jobs with the same k go through one partitioned build: one parse of all their
+ * text, then one bucket space in which every job owns its own contiguous range of buckets
+ * sized from its own distinct-k-mer estimate, so each job's Node set is exactly its
+ * gx_job_run result (records may come in a different order).  Per-job results are read as
+ * usual (gx_job_emit, gx_job_stats); the ms_* and kernel_launches fields describe the whole
+ * pass.  Jobs with GX_ALGO_TABLE, and every job of a pass in which some input fails to parse
+ * (so that each reports its own status and line), run one by one.  Per-job status codes go
+ * to statuses[i] (may be NULL); the call returns the first non-OK status.  Replaces running
+ * one Hyracks job per read set (GenomixHyracksDriver.java:84-135 per sample). */
 gx_status gx_batch_run(gx_ctx *ctx, gx_job **jobs, int n, gx_status *statuses);
 
 /* ---- graph build without device allocation ------------------------------------------- */
