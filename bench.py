@@ -172,6 +172,80 @@ def workload(max_pairs=None):
     return synth.pe_5mbp(max_pairs=max_pairs)
 
 
+def batched_workload(n_samples=64):
+    """The 64-sample batch, generated in a spawn pool (before any CUDA call)."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    from genomix_gb300 import synth
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as ex:
+        return synth.batched_64(n_samples=n_samples, pool=ex)
+
+
+def bench_batched(ctx, samples, steps, warmup, local):
+    """The 64 samples built one job per launch sequence (gx_job_run each) and as one batch
+    (gx_batch_run), text resident in HBM; k-mers/s of each over `steps` repetitions."""
+    import torch
+    import genomix_gb300 as gx
+    dev = [torch.frombuffer(bytearray(w.text), dtype=torch.uint8).to(f"cuda:{local}") for w in samples]
+    torch.cuda.synchronize()
+    k = samples[0].k
+
+    def make_jobs():
+        jobs = []
+        for d in dev:
+            j = gx.GraphBuildJob(ctx, k)
+            j.add_input_device(d.data_ptr(), d.numel())
+            jobs.append(j)
+        return jobs
+
+    def plain():
+        out = []
+        for j in make_jobs():
+            j.run()
+            out.append(j.stats())
+            j.close()
+        return out
+
+    def batched():
+        jobs = make_jobs()
+        sts = gx.batch_run(ctx, jobs)
+        assert all(st == 0 for st in sts), sts
+        out = [j.stats() for j in jobs]
+        for j in jobs:
+            j.close()
+        return out
+
+    for _ in range(warmup):
+        ref = plain()
+        got = batched()
+    # every sample's graph is the same size both ways (the tests check the records themselves)
+    for a, b in zip(ref, got):
+        assert (a["nodes"], a["kmers"], a["read_heads"], a["record_bytes"]) == \
+               (b["nodes"], b["kmers"], b["read_heads"], b["record_bytes"])
+    torch.cuda.synchronize()
+    ctx.mark(4)
+    for _ in range(steps):
+        plain()
+    ctx.mark(5)
+    ms_plain = ctx.elapsed_ms(4, 5) / steps
+    ctx.mark(6)
+    for _ in range(steps):
+        got = batched()
+    ctx.mark(7)
+    ms_batched = ctx.elapsed_ms(6, 7) / steps
+    kmers = sum(st["kmers"] for st in ref)
+    del dev
+    return {"workload": "batched_64_se150_k31", "samples": len(samples), "kmers": kmers,
+            "input_bytes": sum(len(w.text) for w in samples),
+            "nodes": sum(st["nodes"] for st in ref),
+            "plain_kmers_per_s": kmers / (ms_plain / 1e3), "batched_kmers_per_s": kmers / (ms_batched / 1e3),
+            "speedup": ms_plain / ms_batched, "ms_plain": ms_plain, "ms_batched": ms_batched,
+            "gpu_launches_plain": int(sum(st["kernel_launches"] for st in ref)),
+            "gpu_launches_batched": int(got[0]["kernel_launches"]),
+            "batched_phases_ms": {"parse": got[0]["ms_parse"], "partition": got[0]["ms_insert"],
+                                  "aggregate": got[0]["ms_aggregate"], "write": got[0]["ms_write"]}}
+
+
 def config_of(w, n):
     return {"workload": w.name, "genome_bp": w.genome_len, "pairs": w.reads, "read_len": 150, "k": w.k,
             "input_bytes": len(w.text), "parallelism": f"replicas{n}" if n > 1 else "single",
@@ -211,6 +285,7 @@ def run_gb300(args, ws, rank, local):
     import genomix_gb300 as gx
 
     w = workload(args.max_pairs)
+    samples = None if args.no_batched else batched_workload()
     ctx = gx.Context(local)
     torch.cuda.set_device(local)
     d_text = torch.frombuffer(bytearray(w.text), dtype=torch.uint8).to(f"cuda:{local}")
@@ -265,6 +340,10 @@ def run_gb300(args, ws, rank, local):
     ms_e2e = max_over_ranks(ws, ctx.elapsed_ms(2, 3))
     e2e_value = ws * args.steps * kmers / (ms_e2e / 1e3)
 
+    bat = None
+    if samples is not None:
+        bat = bench_batched(ctx, samples, args.steps, args.warmup, local)
+
     if rank != 0:
         return
     peak, peak_kind = peaks()
@@ -302,6 +381,7 @@ def run_gb300(args, ws, rank, local):
                   "read_heads": stats[0]["read_heads"], "record_bytes": out_bytes,
                   "table_slots": stats[0]["table_slots"], "max_probe": stats[0]["max_probe"]},
         "clocks": clk.summary(),
+        "batched": bat,
         "cpu_baseline": cb,
     }
     print(json.dumps(line), flush=True)
@@ -317,6 +397,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-sample batched vs per-job measurement")
     ap.add_argument("--max-pairs", type=int, default=None,
                     help="use only the first pairs of the workload (profiling captures)")
     args = ap.parse_args()

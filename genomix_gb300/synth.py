@@ -196,20 +196,26 @@ def pe_50mbp(max_pairs=None, genome_len=50_000_000):
     return Workload("pe_50mbp_2x250_k55", 55, text, n, True, len(g))
 
 
-def batched_64(n_samples=64, scale=1.0):
-    """64 independent single-end samples (scale < 1 shrinks every genome for tests)."""
-    out = []
-    for s in range(n_samples):
-        rng = rng_for(4, s)
-        G = int(np.exp(rng.uniform(np.log(20_000), np.log(2_000_000))) * scale)
-        G = max(G, 2000)
-        gc = rng.uniform(0.35, 0.60)
-        cov = rng.uniform(10, 60)
-        g = random_genome(rng, G, gc)
-        n = int(round(cov * G / 150))
-        text, n = _build(rng, g, n, 150, False, None, None, 0.005, 0.0)
-        out.append(Workload(f"batched_s{s}", 31, text, n, False, G, {"gc": gc, "coverage": cov}))
-    return out
+def batched_sample(s, scale=1.0):
+    """Sample s of the 64-sample batch: genome log-uniform 20 kbp - 2 Mbp, GC U[0.35, 0.60],
+    coverage U[10, 60], single-end 150 bp, 0.5% substitutions, k = 31."""
+    rng = rng_for(4, s)
+    G = int(np.exp(rng.uniform(np.log(20_000), np.log(2_000_000))) * scale)
+    G = max(G, 2000)
+    gc = rng.uniform(0.35, 0.60)
+    cov = rng.uniform(10, 60)
+    g = random_genome(rng, G, gc)
+    n = int(round(cov * G / 150))
+    text, n = _build(rng, g, n, 150, False, None, None, 0.005, 0.0)
+    return Workload(f"batched_s{s}", 31, text, n, False, G, {"gc": gc, "coverage": cov})
+
+
+def batched_64(n_samples=64, scale=1.0, pool=None):
+    """64 independent single-end samples (scale < 1 shrinks every genome for tests); `pool`
+    (an executor) generates them in parallel, with the same result."""
+    if pool is None:
+        return [batched_sample(s, scale) for s in range(n_samples)]
+    return list(pool.map(batched_sample, range(n_samples), [scale] * n_samples))
 
 
 def serving_jobs(n_jobs, rate_per_s, scale=1.0, seed_sample=0):
