@@ -10,6 +10,7 @@ from .graph import (
     GraphBuildError,
     GraphBuildJob,
     PinnedBuffer,
+    Server,
     batch_run,
     fastq_to_readid,
     iter_records,
@@ -19,6 +20,6 @@ from .graph import (
 )
 
 __all__ = [
-    "Context", "GenomixGpuDriver", "GraphBuildError", "GraphBuildJob", "PinnedBuffer", "batch_run",
+    "Context", "GenomixGpuDriver", "GraphBuildError", "GraphBuildJob", "PinnedBuffer", "Server", "batch_run",
     "fastq_to_readid", "iter_records", "records_to_text", "seqfile_read", "seqfile_write",
 ]

@@ -10,6 +10,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libgxgpu.so")
 
 GX_OK = 0
+GX_EAGAIN = 14
 STATUS_NAMES = {
     0: "GX_OK", 1: "GX_EINVAL", 2: "GX_EINVAL_LINE", 3: "GX_EINVAL_NUMBER", 4: "GX_EREADID_RANGE",
     5: "GX_EREAD_TOO_SHORT", 6: "GX_ENOMEM", 7: "GX_ETABLE_FULL", 8: "GX_ETIMEOUT", 9: "GX_ECUDA",
@@ -25,6 +26,7 @@ EXPORTS = [
     "gx_job_emit_rewind", "gx_job_records_device", "gx_job_stats", "gx_job_destroy", "gx_batch_run", "gx_pinned_alloc",
     "gx_pinned_free", "gx_fastq_to_readid", "gx_host_free", "gx_seqfile_write", "gx_seqfile_read",
     "gx_records_to_text", "gx_build_noalloc",
+    "gx_serve_create", "gx_serve_submit", "gx_serve_poll", "gx_serve_stats_get", "gx_serve_destroy",
 ]
 
 
@@ -45,6 +47,19 @@ class JobOpts(ctypes.Structure):
         ("est_input_bytes", ctypes.c_size_t),
         ("algorithm", ctypes.c_int),
     ]
+
+
+class ServeOpts(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("mem_budget", ctypes.c_size_t), ("lanes", ctypes.c_int),
+                ("max_batch", ctypes.c_int)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("jobs_submitted", "jobs_done", "batches", "max_batch_jobs",
+                                                "jobs_waiting", "jobs_running", "bytes_in_use")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class Stats(ctypes.Structure):
@@ -100,6 +115,11 @@ def load():
         "gx_seqfile_read": ([vp, sz, P(vp), P(sz)], i),
         "gx_records_to_text": ([vp, sz, P(vp), P(sz)], i),
         "gx_build_noalloc": ([i, vp, sz, i, vp, sz, P(sz)], i),
+        "gx_serve_create": ([vp, P(ServeOpts), P(vp)], i),
+        "gx_serve_submit": ([vp, vp, P(ctypes.c_uint64)], i),
+        "gx_serve_poll": ([vp, ctypes.c_uint64, i, P(i), P(ctypes.c_double)], i),
+        "gx_serve_stats_get": ([vp, P(ServeStats)], i),
+        "gx_serve_destroy": ([vp], None),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -333,7 +333,9 @@ gx_status run_group(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         // ---- records of every sample into one buffer ----
         void *outp = nullptr;
         CK(cudaMallocAsync(&outp, total + 16, s));
-        std::shared_ptr<void> owner(outp, [s](void *p) { cudaFreeAsync(p, s); });
+        // freed with the last job that refers to it, by then all its uses on the device are done
+        // (every pass and every emit synchronizes), so any stream may order the free
+        std::shared_ptr<void> owner(outp, [](void *p) { cudaFreeAsync(p, 0); });
         if (((uintptr_t)outp & 15) != 0) return GX_ECUDA;
         EmitArgs a{};
         a.g = TableGeom{nullptr, P, wide};

@@ -1,0 +1,223 @@
+// gx_serve.cu — graph builds served as they arrive (gx_serve_*).
+//
+// A server owns `lanes` contexts on one device, each with its own stream and one worker
+// thread.  Submitted jobs wait in one FIFO queue.  Whenever a lane is idle it admits, in
+// arrival order, every waiting job whose estimated device memory still fits the server's
+// budget (the oldest job is always admitted when nothing else is in flight, so a job larger
+// than the budget still runs, alone), up to `max_batch` jobs, and runs them as one
+// gx_batch_run pass.  Jobs that arrive while lanes are busy are picked up by the next lane
+// to free up: batches form continuously, and the passes of different lanes overlap on the
+// device.  Results stay device-resident in their jobs until the caller emits and destroys
+// them.  While the server runs a job, the job belongs to it: call nothing on that job until
+// gx_serve_poll reports it done.
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/gxgpu.h"
+#include "gx_job_internal.h"
+
+using namespace gxi;
+
+namespace {
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// Device bytes a job needs while it runs, from its input size: occurrences ~ text bytes,
+// two copies of (key + edge bits), node offsets and counts, read heads, the record stream.
+size_t estimate_bytes(const gx_job *j) {
+    size_t text = j->text_len;
+    for (int m = 0; m < 2; m++)
+        for (const std::string &f : j->fastq[m]) text += f.size() / 2;  // a FASTQ record holds its read twice
+    const size_t per_byte = j->k > 32 ? 64 : 44;
+    return text * per_byte + (64u << 20);
+}
+
+struct Ticket {
+    gx_job *job = nullptr;
+    gx_ctx *home = nullptr;
+    size_t est = 0;
+    double t_submit = 0, t_start = 0, t_done = 0;
+    gx_status st = GX_OK;
+    bool done = false;
+};
+
+}  // namespace
+
+struct gx_server {
+    int device = 0;
+    std::vector<gx_ctx *> lanes;
+    std::vector<std::thread> workers;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<uint64_t> pending;
+    std::unordered_map<uint64_t, Ticket> tickets;
+    uint64_t next_id = 1;
+    size_t budget = 0, in_use = 0;
+    int max_batch = 64;
+    int running = 0;
+    bool stop = false;
+    gx_serve_stats stats{};
+};
+
+static void lane_loop(gx_server *sv, gx_ctx *lane) {
+    std::unique_lock<std::mutex> lk(sv->mu);
+    for (;;) {
+        // admit in arrival order while memory lasts
+        std::vector<uint64_t> take;
+        size_t est = 0;
+        for (;;) {
+            take.clear();
+            est = 0;
+            for (uint64_t id : sv->pending) {
+                if ((int)take.size() >= sv->max_batch) break;
+                const size_t e = sv->tickets[id].est;
+                const bool alone = take.empty() && sv->in_use == 0;
+                if (!alone && sv->in_use + est + e > sv->budget) break;  // keep arrival order
+                take.push_back(id);
+                est += e;
+            }
+            if (!take.empty() || (sv->stop && sv->pending.empty())) break;
+            sv->cv_work.wait(lk);
+        }
+        if (take.empty()) return;  // stopping, nothing left
+        for (size_t q = 0; q < take.size(); q++) sv->pending.pop_front();
+        sv->in_use += est;
+        sv->running += (int)take.size();
+        std::vector<gx_job *> jobs;
+        const double t0 = now_ms();
+        for (uint64_t id : take) {
+            Ticket &t = sv->tickets[id];
+            t.t_start = t0;
+            t.job->ctx = lane;  // the lane's stream runs it
+            jobs.push_back(t.job);
+        }
+        sv->stats.batches++;
+        if (take.size() > sv->stats.max_batch_jobs) sv->stats.max_batch_jobs = take.size();
+        lk.unlock();
+        std::vector<gx_status> st(jobs.size(), GX_OK);
+        gx_batch_run(lane, jobs.data(), (int)jobs.size(), st.data());
+        const double t1 = now_ms();
+        lk.lock();
+        for (size_t q = 0; q < take.size(); q++) {
+            Ticket &t = sv->tickets[take[q]];
+            t.job->ctx = t.home;  // every result is complete on the device: the lane synchronized
+            t.st = st[q];
+            t.t_done = t1;
+            t.done = true;
+        }
+        sv->in_use -= est;
+        sv->running -= (int)take.size();
+        sv->stats.jobs_done += take.size();
+        sv->cv_done.notify_all();
+        sv->cv_work.notify_all();
+    }
+}
+
+extern "C" {
+
+gx_status gx_serve_create(gx_ctx *ctx, const gx_serve_opts *opts, gx_server **out) {
+    if (!ctx || !out) return GX_EINVAL;
+    if (opts && opts->struct_size < sizeof(gx_serve_opts)) return GX_EINVAL;
+    *out = nullptr;
+    gx_server *sv = new (std::nothrow) gx_server();
+    if (!sv) return GX_ENOMEM;
+    sv->device = ctx->device;
+    const int lanes = opts && opts->lanes > 0 ? opts->lanes : 2;
+    sv->max_batch = opts && opts->max_batch > 0 ? opts->max_batch : 64;
+    sv->budget = opts && opts->mem_budget ? opts->mem_budget : ctx->mem_limit;
+    for (int i = 0; i < lanes; i++) {
+        gx_ctx_opts co{sizeof(gx_ctx_opts), ctx->mem_limit, 0};
+        gx_ctx *c = nullptr;
+        const gx_status st = gx_ctx_create(ctx->device, &co, &c);
+        if (st != GX_OK) {
+            for (gx_ctx *l : sv->lanes) gx_ctx_destroy(l);
+            delete sv;
+            return st;
+        }
+        sv->lanes.push_back(c);
+    }
+    for (gx_ctx *l : sv->lanes) sv->workers.emplace_back(lane_loop, sv, l);
+    *out = sv;
+    return GX_OK;
+}
+
+gx_status gx_serve_submit(gx_server *sv, gx_job *j, uint64_t *ticket) {
+    if (!sv || !j || !ticket) return GX_EINVAL;
+    if (j->ctx->device != sv->device) return GX_EINVAL;
+    if (j->state != JS_INPUT) return GX_ESTATE;
+    {
+        // the job's inputs were queued on its own context's stream: they must have landed
+        std::lock_guard<std::mutex> lk(j->ctx->mu);
+        cudaSetDevice(j->ctx->device);
+        if (cudaStreamSynchronize(j->ctx->stream) != cudaSuccess) return GX_ECUDA;
+    }
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->stop) return GX_EBUSY;
+    const uint64_t id = sv->next_id++;
+    Ticket t;
+    t.job = j;
+    t.home = j->ctx;
+    t.est = estimate_bytes(j);
+    t.t_submit = now_ms();
+    sv->tickets[id] = t;
+    sv->pending.push_back(id);
+    sv->stats.jobs_submitted++;
+    *ticket = id;
+    sv->cv_work.notify_one();
+    return GX_OK;
+}
+
+gx_status gx_serve_poll(gx_server *sv, uint64_t ticket, int timeout_ms, gx_status *job_status,
+                        double *latency_ms) {
+    if (!sv) return GX_EINVAL;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->tickets.find(ticket);
+    if (it == sv->tickets.end()) return GX_EINVAL;
+    auto ready = [&] { return sv->tickets[ticket].done; };
+    if (!ready()) {
+        if (timeout_ms == 0) return GX_EAGAIN;
+        if (timeout_ms < 0)
+            sv->cv_done.wait(lk, ready);
+        else if (!sv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready))
+            return GX_EAGAIN;
+    }
+    const Ticket t = sv->tickets[ticket];
+    sv->tickets.erase(ticket);
+    if (job_status) *job_status = t.st;
+    if (latency_ms) *latency_ms = t.t_done - t.t_submit;
+    return GX_OK;
+}
+
+gx_status gx_serve_stats_get(gx_server *sv, gx_serve_stats *out) {
+    if (!sv || !out) return GX_EINVAL;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    *out = sv->stats;
+    out->jobs_waiting = sv->pending.size();
+    out->jobs_running = (uint64_t)sv->running;
+    out->bytes_in_use = sv->in_use;
+    return GX_OK;
+}
+
+void gx_serve_destroy(gx_server *sv) {
+    if (!sv) return;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;  // queued jobs still run
+        sv->cv_work.notify_all();
+    }
+    for (std::thread &t : sv->workers) t.join();
+    for (gx_ctx *l : sv->lanes) gx_ctx_destroy(l);
+    delete sv;
+}
+
+}  // extern "C"

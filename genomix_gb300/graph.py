@@ -238,6 +238,60 @@ def batch_run(ctx, jobs):
     return list(sts)
 
 
+class Server:
+    """Graph builds served as they arrive (gx_serve_*): continuous batching by estimated device
+    memory over `lanes` concurrent passes.  submit() hands a job over; poll() returns
+    (status, latency_ms) once it is done, or None while it is not."""
+
+    def __init__(self, ctx, mem_budget=0, lanes=0, max_batch=0):
+        self.ctx = ctx
+        self._L = ctx._L
+        o = _lib.ServeOpts(ctypes.sizeof(_lib.ServeOpts), int(mem_budget), int(lanes), int(max_batch))
+        h = ctypes.c_void_p()
+        _check(self._L.gx_serve_create(ctx.h, ctypes.byref(o), ctypes.byref(h)), "gx_serve_create")
+        self.h = h.value
+        self._jobs = {}
+
+    def submit(self, job):
+        t = ctypes.c_uint64()
+        _check(self._L.gx_serve_submit(self.h, job.h, ctypes.byref(t)), "gx_serve_submit")
+        self._jobs[t.value] = job
+        return t.value
+
+    def poll(self, ticket, timeout_ms=-1):
+        st, lat = ctypes.c_int(), ctypes.c_double()
+        r = self._L.gx_serve_poll(self.h, ticket, int(timeout_ms), ctypes.byref(st), ctypes.byref(lat))
+        if r == _lib.GX_EAGAIN:
+            return None
+        _check(r, "gx_serve_poll")
+        job = self._jobs.pop(ticket, None)
+        if job is not None:
+            job._keep.clear()
+        return st.value, lat.value
+
+    def stats(self):
+        s = _lib.ServeStats()
+        _check(self._L.gx_serve_stats_get(self.h, ctypes.byref(s)), "gx_serve_stats_get")
+        return s.as_dict()
+
+    def close(self):
+        if self.h:
+            self._L.gx_serve_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _buf_out(fn, *args):
     L = _lib.load()
     out, n = ctypes.c_void_p(), ctypes.c_size_t()

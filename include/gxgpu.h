@@ -194,6 +194,48 @@ void gx_job_destroy(gx_job *job);
  * one Hyracks job per read set (GenomixHyracksDriver.java:84-135 per sample). */
 gx_status gx_batch_run(gx_ctx *ctx, gx_job **jobs, int n, gx_status *statuses);
 
+/* ---- serving: graph builds admitted as they arrive ------------------------------------ */
+
+typedef struct gx_server gx_server;
+
+typedef struct gx_serve_opts {
+    size_t struct_size;  /* sizeof(gx_serve_opts) */
+    size_t mem_budget;   /* device bytes the admitted jobs may use together; 0 = the context's limit */
+    int lanes;           /* passes in flight at once, each on its own stream; 0 = 2 */
+    int max_batch;       /* jobs admitted into one pass; 0 = 64 */
+} gx_serve_opts;
+
+typedef struct gx_serve_stats {
+    uint64_t jobs_submitted, jobs_done;
+    uint64_t batches;         /* passes run */
+    uint64_t max_batch_jobs;  /* most jobs admitted into one pass */
+    uint64_t jobs_waiting, jobs_running;
+    uint64_t bytes_in_use;    /* estimated device bytes of the running jobs */
+} gx_serve_stats;
+
+/* Start a server on ctx's device.  Each lane is a context of its own with one worker thread.
+ * An idle lane admits, in arrival order, every waiting job whose estimated device memory
+ * (from its input size) fits the budget next to the jobs already running, up to max_batch,
+ * and runs them as one gx_batch_run pass; jobs that arrive meanwhile wait for the next free
+ * lane, so batches form continuously and the lanes' passes overlap on the device.  The
+ * oldest waiting job is always admitted when nothing runs.  Replaces submitting one
+ * GenomixHyracksDriver.runJob (GenomixHyracksDriver.java:84-135) per request; the
+ * reference has no serving mode. */
+gx_status gx_serve_create(gx_ctx *ctx, const gx_serve_opts *opts, gx_server **out);
+/* Hand a job with its inputs added (not yet run) to the server.  The job belongs to the
+ * server until gx_serve_poll reports it done: make no call on it before that.  Its results
+ * then stay device-resident in the job (gx_job_emit, gx_job_records_device) until
+ * gx_job_destroy.  GX_EBUSY once the server is being destroyed. */
+gx_status gx_serve_submit(gx_server *srv, gx_job *job, uint64_t *ticket);
+/* Wait up to timeout_ms (0: do not wait, < 0: wait until done) for a ticket.  GX_EAGAIN if
+ * it is not done yet; GX_OK once done, with the job's own status and its latency from
+ * submission to completion (the ticket is then released). */
+gx_status gx_serve_poll(gx_server *srv, uint64_t ticket, int timeout_ms, gx_status *job_status,
+                        double *latency_ms);
+gx_status gx_serve_stats_get(gx_server *srv, gx_serve_stats *out);
+/* Runs every job still queued, then stops the lanes. */
+void gx_serve_destroy(gx_server *srv);
+
 /* ---- graph build without device allocation ------------------------------------------- */
 
 /* Bytes of the device scratch array behind gx_build_noalloc. */
