@@ -20,6 +20,11 @@ reads, see genomix_gb300/synth.py).
              k-mers/s against the hash-table random-access bound (64 B per occurrence)
   cpu_baseline  the oracle (C++ restatement of the reference's sort + group graph build) on
              the first pairs of the same workload, all host threads
+  batched    the 64-sample workload (genomes log-uniform 20 kbp - 2 Mbp, 10-60x single-end
+             150 bp, k = 31) built one gx_job_run per sample and as one gx_batch_run pass
+  serving    a Poisson stream of jobs (genomes log-uniform 10 kbp - 5 Mbp, 30x, 2 x 150 bp
+             pairs, k in {21, 31, 55}) through gx_serve_*, offered rate swept: p50/p99
+             latency from arrival to completion and k-mers/s per rate
 
 With --impl reference the oracle itself is the measured implementation (the reference is
 Java 7 on Hyracks and cannot run on the box).  With N > 1 (torchrun) every rank builds its
@@ -181,6 +186,83 @@ def batched_workload(n_samples=64):
         return synth.batched_64(n_samples=n_samples, pool=ex)
 
 
+def serving_workload(n_pool=48):
+    """A pool of distinct serving jobs, generated in a spawn pool (before any CUDA call)."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    from genomix_gb300 import synth
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as ex:
+        return [w for _, w in synth.serving_jobs(n_pool, 1.0, pool=ex)]
+
+
+SERVE_RATES = (25, 50, 100, 200, 400, 800)  # offered jobs/s
+SERVE_REQUESTS = 96                         # requests per rate, cycling through the job pool
+SERVE_CLIENTS = 4                           # client threads submitting the arrivals
+
+
+def bench_serving(ctx, works, rates=SERVE_RATES, n_req=SERVE_REQUESTS):
+    """Poisson arrivals of graph-build jobs at each offered rate: client threads create each
+    job at its arrival time (input copied from pinned host memory) and hand it to the server;
+    the results stay on the device.  Latency runs from arrival to completion."""
+    import threading
+    import genomix_gb300 as gx
+    from genomix_gb300 import synth
+    pins = []
+    for w in works:
+        p = gx.PinnedBuffer(len(w.text))
+        p.array()[:] = memoryview(w.text)
+        pins.append(p)
+    out = []
+    with gx.Server(ctx) as srv:
+        for rate in rates:
+            arr = synth.poisson_arrivals(n_req, rate, seed_sample=1)
+            tickets, jobs, t_sub = [None] * n_req, [None] * n_req, [0.0] * n_req
+            ready = [threading.Event() for _ in range(n_req)]
+            t0 = time.perf_counter() + 0.01
+
+            def submitter(first):
+                for i in range(first, n_req, SERVE_CLIENTS):
+                    dt = t0 + arr[i] - time.perf_counter()
+                    if dt > 0:
+                        time.sleep(dt)
+                    q = i % len(works)
+                    j = gx.GraphBuildJob(ctx, works[q].k)
+                    j.add_input(pins[q])
+                    jobs[i] = j
+                    tickets[i] = srv.submit(j)
+                    t_sub[i] = time.perf_counter()
+                    ready[i].set()
+
+            ths = [threading.Thread(target=submitter, args=(c,)) for c in range(SERVE_CLIENTS)]
+            for th in ths:
+                th.start()
+            lat, kmers, t_end = [], 0, t0
+            for i in range(n_req):
+                ready[i].wait()
+                st, srv_ms = srv.poll(tickets[i])
+                assert st == 0, st
+                lt = (t_sub[i] - (t0 + arr[i])) * 1e3 + srv_ms  # arrival -> done
+                lat.append(lt)
+                t_end = max(t_end, t0 + arr[i] + lt / 1e3)
+                kmers += jobs[i].stats()["kmers"]
+                jobs[i].close()
+            for th in ths:
+                th.join()
+            span = t_end - t0
+            lat.sort()
+            out.append({"offered_jobs_per_s": rate, "jobs": n_req, "achieved_jobs_per_s": n_req / span,
+                        "kmers_per_s": kmers / span, "p50_ms": lat[len(lat) // 2],
+                        "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))]})
+        st = srv.stats()
+    for p in pins:
+        p.close()
+    sustained = [r for r in out if r["achieved_jobs_per_s"] >= 0.9 * r["offered_jobs_per_s"]]
+    top = max(sustained, key=lambda r: r["offered_jobs_per_s"]) if sustained else None
+    return {"workload": "serving_pe150_30x_k21_31_55", "job_pool": len(works),
+            "mean_job_bytes": sum(len(w.text) for w in works) / len(works), "rates": out,
+            "highest_sustained": top, "passes": st["batches"], "max_jobs_per_pass": st["max_batch_jobs"]}
+
+
 def bench_batched(ctx, samples, steps, warmup, local):
     """The 64 samples built one job per launch sequence (gx_job_run each) and as one batch
     (gx_batch_run), text resident in HBM; k-mers/s of each over `steps` repetitions."""
@@ -286,6 +368,7 @@ def run_gb300(args, ws, rank, local):
 
     w = workload(args.max_pairs)
     samples = None if args.no_batched else batched_workload()
+    serve_pool = None if args.no_serving else serving_workload()
     ctx = gx.Context(local)
     torch.cuda.set_device(local)
     d_text = torch.frombuffer(bytearray(w.text), dtype=torch.uint8).to(f"cuda:{local}")
@@ -340,9 +423,12 @@ def run_gb300(args, ws, rank, local):
     ms_e2e = max_over_ranks(ws, ctx.elapsed_ms(2, 3))
     e2e_value = ws * args.steps * kmers / (ms_e2e / 1e3)
 
-    bat = None
+    bat = srv = None
     if samples is not None:
         bat = bench_batched(ctx, samples, args.steps, args.warmup, local)
+        del samples
+    if serve_pool is not None:
+        srv = bench_serving(ctx, serve_pool)
 
     if rank != 0:
         return
@@ -382,6 +468,7 @@ def run_gb300(args, ws, rank, local):
                   "table_slots": stats[0]["table_slots"], "max_probe": stats[0]["max_probe"]},
         "clocks": clk.summary(),
         "batched": bat,
+        "serving": srv,
         "cpu_baseline": cb,
     }
     print(json.dumps(line), flush=True)
@@ -398,6 +485,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-sample batched vs per-job measurement")
+    ap.add_argument("--no-serving", action="store_true", help="skip the served-stream measurement")
     ap.add_argument("--max-pairs", type=int, default=None,
                     help="use only the first pairs of the workload (profiling captures)")
     args = ap.parse_args()

@@ -218,21 +218,34 @@ def batched_64(n_samples=64, scale=1.0, pool=None):
     return list(pool.map(batched_sample, range(n_samples), [scale] * n_samples))
 
 
-def serving_jobs(n_jobs, rate_per_s, scale=1.0, seed_sample=0):
-    """(arrival_s, Workload) for a Poisson stream of graph-build jobs."""
+def serving_job(i, scale=1.0, seed_sample=0):
+    """Job i of the serving stream: genome log-uniform 10 kbp - 5 Mbp at 30x, 2 x 150 bp pairs,
+    insert N(400, 40), 0.8% substitutions, k drawn from {21, 31, 55}."""
+    r = rng_for(5, seed_sample * 100_000 + i)
+    G = max(2000, int(np.exp(r.uniform(np.log(10_000), np.log(5_000_000))) * scale))
+    k = int(r.choice([21, 31, 55]))
+    g = random_genome(r, G, 0.5)
+    pairs = int(round(30 * G / 300))
+    text, n = _build(r, g, pairs, 150, True, 400, 40, 0.008, 0.0)
+    return Workload(f"serve_{i}", k, text, n, True, G)
+
+
+def poisson_arrivals(n_jobs, rate_per_s, seed_sample=0):
+    """Arrival times (s) of a Poisson stream at rate_per_s."""
     rng = rng_for(5, 10_000 + seed_sample)
-    gaps = rng.exponential(1.0 / rate_per_s, size=n_jobs)
-    t = np.cumsum(gaps)
-    jobs = []
-    for i in range(n_jobs):
-        r = rng_for(5, seed_sample * 100_000 + i)
-        G = max(2000, int(np.exp(r.uniform(np.log(10_000), np.log(5_000_000))) * scale))
-        k = int(r.choice([21, 31, 55]))
-        g = random_genome(r, G, 0.5)
-        pairs = int(round(30 * G / 300))
-        text, n = _build(r, g, pairs, 150, True, 400, 40, 0.008, 0.0)
-        jobs.append((float(t[i]), Workload(f"serve_{i}", k, text, n, True, G)))
-    return jobs
+    return np.cumsum(rng.exponential(1.0 / rate_per_s, size=n_jobs))
+
+
+def serving_jobs(n_jobs, rate_per_s, scale=1.0, seed_sample=0, pool=None):
+    """(arrival_s, Workload) for a Poisson stream of graph-build jobs; `pool` (an executor)
+    generates the jobs in parallel, with the same result."""
+    t = poisson_arrivals(n_jobs, rate_per_s, seed_sample)
+    idx = list(range(n_jobs))
+    if pool is None:
+        works = [serving_job(i, scale, seed_sample) for i in idx]
+    else:
+        works = list(pool.map(serving_job, idx, [scale] * n_jobs, [seed_sample] * n_jobs))
+    return [(float(t[i]), works[i]) for i in idx]
 
 
 def small_random(seed, n_reads, read_len, k, paired=False, genome_len=2000, err=0.01, n_rate=0.0, gc=0.5):
