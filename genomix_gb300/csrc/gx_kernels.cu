@@ -2064,157 +2064,83 @@ void launch_aggregate(const AggArgs &a, cudaStream_t s) {
 }
 
 // ---- D: record writer of the partitioned build ------------------------------------------------
-// Each warp writes the records of a contiguous node range through a private window of
-// shared memory; node offsets and read-head positions come precomputed, so no block-wide
-// barrier is needed.  A node lane writes frame, key, active byte, edges and coverage with
-// whole-word stores (WordWriter); the read-head sets are written warp-cooperatively.
+// Each warp writes the records of a contiguous node range.  It cuts the range into windows
+// that end on record boundaries and hold at most WARP_STAGE bytes, assembles each window in
+// a private piece of shared memory and copies it out with aligned 16-byte stores.  Inside a
+// window, lane i of an iteration writes record j0 + i: every word that lies wholly inside its
+// record is stored as soon as it fills, and the word two neighbouring records share (the
+// previous record's tail and this one's head) is put together with a warp shuffle and
+// stored once, so no word is written by two lanes and nothing has to be cleared first.  The
+// read-head sets are written warp-cooperatively afterwards, byte by byte, into the gaps
+// the records leave for them.  A record larger than a window (a node with very many read
+// heads) is written alone, byte by byte, over as many windows as it needs.
 constexpr uint32_t WARP_STAGE = 6144;
 constexpr int WRITER_WARPS = 8;
 
-// Big-endian fields at byte positions of a shared window.  A record's words are stored
-// whole; the word it shares with its predecessor (its first word, when it starts mid-word)
-// and the word it shares with its successor (its trailing partial word) are merged with
-// atomicOr into words zeroed beforehand.
-struct WordWriter {
+// Bytes appended in memory order through a 32-bit accumulator.  The record's first word,
+// when the record starts mid-word, is kept in `first` instead of being stored (it holds the
+// predecessor's tail too); the trailing partial word stays in `cur`.
+struct RecAcc {
     uint32_t *w;
-    uint32_t pos;    // next byte position (window-relative)
-    uint32_t cur;    // pending bytes of word pos >> 2, in memory order from the low byte
-    bool merge_first;  // the next word flushed is shared with the predecessor
-    __device__ __forceinline__ void begin(uint32_t *w_, uint32_t p, bool shared_start) {
+    uint32_t wi;    // word being filled
+    uint32_t fill;  // bytes of that word already in cur (0..3)
+    uint32_t cur;
+    uint32_t fw;    // the record's first word
+    uint32_t first;
+    bool hold_first;
+    __device__ __forceinline__ void init(uint32_t *w_, uint32_t pos) {
         w = w_;
-        pos = p;
-        cur = 0;
-        merge_first = shared_start && (p & 3) != 0;
-    }
-    __device__ __forceinline__ void put_word(uint32_t wi, uint32_t v) {
-        if (merge_first) {
-            atomicOr(&w[wi], v);
-            merge_first = false;
-        } else {
-            w[wi] = v;
-        }
-    }
-    __device__ __forceinline__ void byte(uint32_t b) {
-        cur |= (b & 0xffu) << (8 * (pos & 3));
-        pos++;
-        if ((pos & 3) == 0) {
-            put_word((pos >> 2) - 1, cur);
-            cur = 0;
-        }
-    }
-    __device__ __forceinline__ void be32(uint32_t v) {
-        const uint32_t le = __byte_perm(v, 0, 0x0123);  // the 4 bytes in memory order
-        const uint32_t off = pos & 3;
-        if (off == 0) {
-            put_word(pos >> 2, le);
-        } else {
-            put_word(pos >> 2, cur | (le << (8 * off)));
-            cur = le >> (32 - 8 * off);
-        }
-        pos += 4;
-    }
-    // pending bytes of a partial last word: merged if the word is shared with the next
-    // record, stored otherwise (the rest of the word belongs to this record)
-    __device__ __forceinline__ void end(bool shared) {
-        if (pos & 3) {
-            if (shared || merge_first)
-                atomicOr(&w[pos >> 2], cur);
-            else
-                w[pos >> 2] = cur;
-        }
-    }
-};
-
-// Bytes appended in memory order to a shared window through a 64-bit accumulator: one
-// word store per 4 bytes.  The first word is merged with atomicOr when the record starts
-// mid-word (it holds the predecessor's last bytes); finish() merges the trailing partial
-// word when it is shared with the next record.
-struct ByteAcc {
-    uint32_t *w;
-    uint32_t wi;       // word the accumulator fills
-    uint32_t first;    // record's first word
-    uint32_t fill;     // bytes in acc
-    bool merge_first;
-    unsigned long long acc;
-    __device__ __forceinline__ void init(uint32_t *w_, uint32_t pos, bool shared_start) {
-        w = w_;
-        wi = pos >> 2;
-        first = wi;
+        wi = fw = pos >> 2;
         fill = pos & 3;
-        merge_first = shared_start && fill != 0;
-        acc = 0;
+        cur = first = 0;
+        hold_first = fill != 0;
     }
-    __device__ __forceinline__ void store(uint32_t v) {
-        if (merge_first && wi == first)
-            atomicOr(&w[wi], v);
-        else
-            w[wi] = v;
-    }
-    // n <= 4 bytes, the first in the low byte of le
+    // n (1..4) bytes, the first in the low byte of le, the bytes above n zero
     __device__ __forceinline__ void put(uint32_t le, uint32_t n) {
-        acc |= (unsigned long long)le << (8 * fill);
+        const uint32_t sh = fill * 8;
+        const uint32_t lo = cur | (le << sh);
         fill += n;
         if (fill >= 4) {
-            store((uint32_t)acc);
+            if (hold_first && wi == fw)
+                first = lo;
+            else
+                w[wi] = lo;
             wi++;
-            acc >>= 32;
             fill -= 4;
+            cur = __funnelshift_rc(le, 0u, 32 - sh);  // the bytes that spill into the next word
+        } else {
+            cur = lo;
         }
     }
     __device__ __forceinline__ void be32(uint32_t v) { put(__byte_perm(v, 0, 0x0123), 4); }
-    __device__ __forceinline__ void byte(uint32_t b) { put(b & 0xffu, 1); }
-    __device__ __forceinline__ void finish(bool shared_end) {
-        if (fill) {
-            if (shared_end || (merge_first && wi == first))
-                atomicOr(&w[wi], (uint32_t)acc);
-            else
-                w[wi] = (uint32_t)acc;
-        }
-    }
 };
 
-// nb bytes of a k-mer value, big-endian, in groups of up to 4
-template <class K>
-__device__ __forceinline__ void acc_kbytes(ByteAcc &o, K v, int nb) {
-    for (int rem = nb; rem > 0; rem -= 4) {
-        const int n = rem < 4 ? rem : 4;
-        const uint32_t chunk = (uint32_t)(v >> (8 * (rem - n))) << (8 * (4 - n));  // BE bytes at the top
-        o.put(__byte_perm(chunk, 0, 0x0123), (uint32_t)n);
-    }
+// the nb big-endian bytes of a k-mer value, as little-endian words in memory order
+__device__ __forceinline__ void key_words(uint64_t v, int nb, uint32_t w[4]) {
+    const uint64_t u = v << (64 - 8 * nb);
+    w[0] = __byte_perm((uint32_t)(u >> 32), 0, 0x0123);
+    w[1] = __byte_perm((uint32_t)u, 0, 0x0123);
+    w[2] = w[3] = 0;
+}
+__device__ __forceinline__ void key_words(u128 v, int nb, uint32_t w[4]) {
+    const u128 u = v << (128 - 8 * nb);
+    const uint64_t hi = (uint64_t)(u >> 64), lo = (uint64_t)u;
+    w[0] = __byte_perm((uint32_t)(hi >> 32), 0, 0x0123);
+    w[1] = __byte_perm((uint32_t)hi, 0, 0x0123);
+    w[2] = __byte_perm((uint32_t)(lo >> 32), 0, 0x0123);
+    w[3] = __byte_perm((uint32_t)lo, 0, 0x0123);
 }
 
-// nb bytes of a k-mer value, big-endian (VKmer bytes after the header)
 template <class K>
-__device__ __forceinline__ void ww_kbytes(WordWriter &o, K v, int nb) {
-    int rem = nb;
-    while (rem >= 4) {
-        o.be32((uint32_t)(v >> (8 * (rem - 4))));
-        rem -= 4;
-    }
-    while (rem > 0) {
-        rem--;
-        o.byte((uint32_t)(v >> (8 * rem)));
+__device__ __forceinline__ void put_key(RecAcc &o, K v, int nb) {
+    uint32_t w[4];
+    key_words(v, nb, w);
+#pragma unroll
+    for (int q = 0; q < (sizeof(K) == 8 ? 2 : 4); q++) {
+        const int rem = nb - 4 * q;
+        if (rem > 0) o.put(w[q], rem < 4 ? (uint32_t)rem : 4u);
     }
 }
-
-// The same record fields with per-byte window checks, merging every byte with atomicOr
-// (records that straddle two windows).
-struct OrSink {
-    uint32_t *w;
-    long long lo, hi;
-    __device__ __forceinline__ void b(long long pos, uint32_t v) const {
-        if (pos >= lo && pos < hi) {
-            const uint32_t q = (uint32_t)(pos - lo);
-            atomicOr(&w[q >> 2], (v & 0xffu) << (8 * (q & 3)));
-        }
-    }
-    __device__ __forceinline__ void u32(long long pos, uint32_t v) const {
-        b(pos, v >> 24);
-        b(pos + 1, v >> 16);
-        b(pos + 2, v >> 8);
-        b(pos + 3, v);
-    }
-};
 
 template <class K>
 __device__ __forceinline__ void node_neighbors(K key, uint32_t m, int t, int k, K y[4], int &ny) {
@@ -2229,12 +2155,10 @@ __device__ __forceinline__ void node_neighbors(K key, uint32_t m, int t, int k, 
         }
 }
 
-// a record that crosses a window edge: byte by byte, merged with atomicOr (rare)
+// a record larger than a window: byte by byte, only the bytes inside the window
 template <class K>
-__device__ __forceinline__ void write_record_straddling(uint32_t *stage32, long long W, long long wend, long long st,
-                                                     long long en, K key, uint32_t meta, uint32_t active, uint32_t cov,
-                                                     int k, int nb) {
-    const OrSink o{stage32, W, wend};
+__device__ __noinline__ void write_record_bytes(const Sink &o, long long st, long long en, K key, uint32_t meta,
+                                                uint32_t active, uint32_t cov, int k, int nb) {
     o.u32(st, (uint32_t)(en - st - 8));
     o.u32(st + 4, (uint32_t)(4 + nb));
     o.u32(st + 8, (uint32_t)k);
@@ -2260,21 +2184,9 @@ __device__ __forceinline__ void write_record_straddling(uint32_t *stage32, long 
     o.u32(en - 4, cov);
 }
 
-// a list with 2..4 neighbours (a branching node), sorted ascending
-template <class K>
-__device__ __forceinline__ void acc_branch_list(ByteAcc &o, K key, uint32_t m, int t, int k, int nb) {
-    K y[4];
-    int c;
-    node_neighbors<K>(key, m, t, k, y, c);
-    for (int u = 0; u < c; u++) {
-        o.be32((uint32_t)k);
-        acc_kbytes<K>(o, y[u], nb);
-    }
-}
-
-// the read-head sets of the warp's heads inside the window
+// the read-head sets of heads [hlo, hhi) that touch the window
 __device__ __forceinline__ void write_heads_window(const Sink &ow, const HeadOut *hout, uint32_t hlo, uint32_t hhi,
-                                                const uint8_t *text, int lane) {
+                                                   const uint8_t *text, int lane) {
     for (uint32_t h = hlo; h < hhi; h++) {
         const HeadOut ho = hout[h];
         const uint32_t nbr = packed_len(ho.L), nbm = packed_len(ho.Lm);
@@ -2297,6 +2209,45 @@ __device__ __forceinline__ void write_heads_window(const Sink &ow, const HeadOut
     }
 }
 
+// first head at or after partition-local position x (heads are sorted by position)
+__device__ __forceinline__ uint32_t head_lower_bound(const HeadOut *hout, uint32_t hc, unsigned long long x) {
+    uint32_t lo = 0, hi = hc;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if ((unsigned long long)hout[mid].pos < x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// window [W, wend) of the partition out to global memory with aligned 16-byte stores
+__device__ __forceinline__ void window_out(uint8_t *out, const uint8_t *stage, unsigned long long g0,
+                                           unsigned long long g1, int lane) {
+    const uint32_t *stage32 = reinterpret_cast<const uint32_t *>(stage);
+    for (unsigned long long c = (g0 & ~15ULL) + 16ULL * lane; c < g1; c += 16ULL * 32) {
+        if (c >= g0 && c + 16 <= g1) {
+            const uint32_t ofs = (uint32_t)(c - g0);
+            const uint32_t w0 = ofs >> 2, sh = (ofs & 3u) * 8u;
+            uint32_t w[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) w[q] = stage32[w0 + q];
+            uint4 v;
+            v.x = __funnelshift_r(w[0], w[1], sh);
+            v.y = __funnelshift_r(w[1], w[2], sh);
+            v.z = __funnelshift_r(w[2], w[3], sh);
+            v.w = __funnelshift_r(w[3], w[4], sh);
+            *reinterpret_cast<uint4 *>(out + c) = v;
+        } else {
+            for (int q = 0; q < 16; q++) {
+                const unsigned long long g = c + q;
+                if (g >= g0 && g < g1) out[g] = stage[g - g0];
+            }
+        }
+    }
+}
+
 template <class K>
 __global__ void __launch_bounds__(WRITER_WARPS * 32, 3) k_emit_write_part(EmitArgs a) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
@@ -2316,125 +2267,127 @@ __global__ void __launch_bounds__(WRITER_WARPS * 32, 3) k_emit_write_part(EmitAr
     const HeadOut *hout = a.hout + hb;
     const uint32_t npw = (n + WRITER_WARPS - 1) / WRITER_WARPS;
     const uint32_t j0 = min(n, warp * npw), j1 = min(n, j0 + npw);
-    if (j0 >= j1) return;
-    const unsigned long long wlo = noff[j0];
-    const unsigned long long whi = j1 < n ? (unsigned long long)noff[j1] : pbytes;
-    // this warp's heads: those positioned inside [wlo, whi) (sorted by position)
-    uint32_t hlo = 0, hhi = 0;
-    for (uint32_t i0 = 0; i0 < hc; i0 += 32) {
-        const uint32_t i = i0 + lane;
-        const unsigned long long hp = i < hc ? (unsigned long long)hout[i].pos : ~0ULL;
-        hlo += __popc(__ballot_sync(0xffffffffu, i < hc && hp < wlo));
-        hhi += __popc(__ballot_sync(0xffffffffu, i < hc && hp < whi));
-    }
-    const uint32_t iters = (j1 - j0 + 31) / 32;
-    for (unsigned long long W = wlo; W < whi; W += WARP_STAGE) {
-        const unsigned long long wend = min(whi, W + WARP_STAGE);
+    // record j starts at off_at(j); off_at(n) is the partition's end
+    auto off_at = [&](uint32_t j) -> unsigned long long {
+        return j < n ? (unsigned long long)noff[j] : pbytes;
+    };
+    const unsigned full = 0xffffffffu;
+    uint32_t ja = j0;
+    while (ja < j1) {
+        const unsigned long long W = off_at(ja);
+        if (off_at(ja + 1) - W > WARP_STAGE) {
+            // ---- one record larger than a window ----
+            const unsigned long long en = off_at(ja + 1);
+            const unsigned long long cm = ncm[ja];
+            const uint32_t meta = (uint32_t)(cm >> 32);
+            uint32_t active = 0x80u;
+            for (int t = 0; t < 4; t++)
+                if ((meta >> (4 * t)) & 15u) active |= 1u << t;
+            if (meta & META_UNFLIPPED) active |= 0x10u;
+            if (meta & META_FLIPPED) active |= 0x20u;
+            const uint32_t cov = __float_as_uint((float)(uint32_t)cm);
+            const K key = nkey[ja];
+            const uint32_t hlo = head_lower_bound(hout, hc, W), hhi = head_lower_bound(hout, hc, en);
+            for (unsigned long long Wg = W; Wg < en; Wg += WARP_STAGE) {
+                const unsigned long long we = min(en, Wg + WARP_STAGE);
+                const Sink o{stage, (long long)Wg, (long long)we, false};
+                if (lane == 0) write_record_bytes<K>(o, (long long)W, (long long)en, key, meta, active, cov, k, nb);
+                __syncwarp();
+                write_heads_window(o, hout, hlo, hhi, a.text, lane);
+                __syncwarp();
+                window_out(a.out, stage, base + Wg, base + we, lane);
+                __syncwarp();
+            }
+            ja++;
+            continue;
+        }
+        // ---- records [ja, jb): the most that fit in one window ----
+        uint32_t lo = ja + 1, hi = j1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (off_at(mid) - W <= WARP_STAGE)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const uint32_t jb = lo;
+        const unsigned long long wend = off_at(jb);
+        const uint32_t iters = (jb - ja + 31) / 32;
+        uint32_t carry = 0;  // tail bytes of the previous iteration's last record
         for (uint32_t it = 0; it < iters; it++) {
-            const uint32_t j = j0 + lane + 32 * it;
-            long long st = -1, en = 0;
-            K key = 0;
-            unsigned long long cm = 0;
-            if (j < j1) {
-                st = noff[j];
-                en = j + 1 < n ? (long long)noff[j + 1] : (long long)pbytes;
-                key = nkey[j];
-                cm = ncm[j];
-            }
-            const bool live = st >= 0 && st < (long long)wend && en > (long long)W;
-            const bool whole = live && st >= (long long)W && en <= (long long)wend;
-            // Zero the words merged with atomicOr.  A record zeroes its trailing word (shared
-            // with its successor, written in this or a later iteration), the record opening
-            // the window zeroes word 0, a record crossing a window edge zeroes the words it
-            // owns alone.  A record never zeroes a first word that holds a predecessor's bytes.
+            const uint32_t j = ja + 32 * it + lane;
+            const bool live = j < jb;
+            uint32_t st = 0, en = 0, lv = 0, first = 0;
             if (live) {
-                const long long fw = (max(st, (long long)W) - (long long)W) >> 2;
-                const long long lw = (min(en, (long long)wend) - 1 - (long long)W) >> 2;
-                // (a record crossing the window end with <= 4 bytes inside has lw == fw,
-                //  which may already hold its predecessor's bytes)
-                const bool shared_first = st > (long long)W && ((st - (long long)W) & 3) != 0;
-                if (!(lw == fw && shared_first)) stage32[lw] = 0;
-                if (st <= (long long)W) stage32[0] = 0;
-                if (!whole) {
-                    if (((st - (long long)W) & 3) == 0) stage32[fw] = 0;  // not shared when aligned
-                    for (long long q2 = fw + 1; q2 < lw; q2++) stage32[q2] = 0;
-                }
-            }
-            __syncwarp();
-            if (live) {
+                st = (uint32_t)(noff[j] - W);
+                en = (uint32_t)(off_at(j + 1) - W);
+                const K key = nkey[j];
+                const unsigned long long cm = ncm[j];
                 const uint32_t meta = (uint32_t)(cm >> 32);
                 uint32_t active = 0x80u;
 #pragma unroll
                 for (int t = 0; t < 4; t++)
                     if ((meta >> (4 * t)) & 15u) active |= 1u << t;
+                const bool heads = (meta & (META_UNFLIPPED | META_FLIPPED)) != 0;
                 if (meta & META_UNFLIPPED) active |= 0x10u;
                 if (meta & META_FLIPPED) active |= 0x20u;
-                const uint32_t cov = __float_as_uint((float)(uint32_t)cm);
-                if (whole) {
-                    // whole record in the window: word stores
-                    const uint32_t rs = (uint32_t)(st - (long long)W), re = (uint32_t)(en - (long long)W);
-                    ByteAcc o;
-                    o.init(stage32, rs, true);
-                    o.be32((uint32_t)(en - st - 8));
-                    o.be32((uint32_t)(4 + nb));
-                    o.be32((uint32_t)k);
-                    acc_kbytes<K>(o, key, nb);
-                    o.byte(active);
-                    // present edge lists, walked uniformly: one list per step
-                    uint32_t lists = active & 15u;
-                    const uint32_t nl = __popc(lists);
-                    for (uint32_t li = 0; li < nl; li++) {
-                        const int t = __ffs(lists) - 1;
-                        lists &= lists - 1;
-                        const uint32_t m = (meta >> (4 * t)) & 15u;
-                        const int ny = __popc(m);
-                        o.be32((uint32_t)ny);
-                        if (ny == 1) {
+                const uint32_t cov_le = __byte_perm(__float_as_uint((float)(uint32_t)cm), 0, 0x0123);
+                RecAcc o;
+                o.init(stage32, st);
+                o.be32(en - st - 8);
+                o.be32((uint32_t)(4 + nb));
+                o.be32((uint32_t)k);
+                put_key<K>(o, key, nb);
+                o.put(active, 1);
+                uint32_t lists = active & 15u;
+                while (lists) {
+                    const int t = __ffs(lists) - 1;
+                    lists &= lists - 1;
+                    const uint32_t m = (meta >> (4 * t)) & 15u;
+                    const int ny = __popc(m);
+                    o.be32((uint32_t)ny);
+                    if (ny == 1) {
+                        o.be32((uint32_t)k);
+                        put_key<K>(o, edge_neighbor<K>(key, t, __ffs(m) - 1, k), nb);
+                    } else {
+                        K y[4];
+                        int c;
+                        node_neighbors<K>(key, m, t, k, y, c);
+                        for (int u = 0; u < c; u++) {
                             o.be32((uint32_t)k);
-                            acc_kbytes<K>(o, edge_neighbor<K>(key, t, __ffs(m) - 1, k), nb);
-                        } else {
-                            acc_branch_list<K>(o, key, m, t, k, nb);
+                            put_key<K>(o, y[u], nb);
                         }
                     }
-                    if ((o.wi << 2) + o.fill != re - 4) {  // read-head sets follow (written below)
-                        o.finish(false);
-                        o.init(stage32, re - 4, false);
-                    }
-                    o.be32(cov);
-                    o.finish(true);
-                } else {
-                    write_record_straddling<K>(stage32, (long long)W, (long long)wend, st, en, key, meta, active, cov, k,
-                                               nb);
                 }
+                if (!heads) {
+                    o.put(cov_le, 4);
+                    lv = o.fill ? o.cur : 0u;
+                } else {
+                    // the head sets fill [lists end, en - 4): store the partial word that
+                    // ends the lists (its other bytes come with the heads), then the coverage
+                    // bytes; the coverage's tail word is shared with the next record
+                    if (o.fill) stage32[o.wi] = o.cur;
+#pragma unroll
+                    for (int q = 0; q < 4; q++) stage[en - 4 + q] = (uint8_t)(cov_le >> (8 * q));
+                    lv = (en & 3) ? cov_le >> (8 * (4 - (en & 3))) : 0u;
+                }
+                first = o.first;
             }
-            __syncwarp();
+            // the word shared with the previous record: its tail bytes | this record's head
+            uint32_t prev = __shfl_up_sync(full, lv, 1);
+            if (lane == 0) prev = carry;
+            if (live && (st & 3)) stage32[st >> 2] = first | prev;
+            // the window's last record keeps its own tail word
+            if (live && j == jb - 1 && (en & 3)) stage32[en >> 2] = lv;
+            carry = __shfl_sync(full, lv, 31);
         }
-        // read heads: set header, flags, uuid, lengths, packed letters
+        __syncwarp();
+        const uint32_t hlo = head_lower_bound(hout, hc, W), hhi = head_lower_bound(hout, hc, wend);
         if (hlo < hhi) write_heads_window(Sink{stage, (long long)W, (long long)wend, false}, hout, hlo, hhi, a.text, lane);
         __syncwarp();
-        // window out with aligned 16-byte stores
-        const unsigned long long g0 = base + W, g1 = base + wend;
-        for (unsigned long long c = (g0 & ~15ULL) + 16ULL * lane; c < g1; c += 16ULL * 32) {
-            if (c >= g0 && c + 16 <= g1) {
-                const uint32_t ofs = (uint32_t)(c - g0);
-                const uint32_t w0 = ofs >> 2, sh = (ofs & 3u) * 8u;
-                uint32_t w[5];
-#pragma unroll
-                for (int q = 0; q < 5; q++) w[q] = stage32[w0 + q];
-                uint4 v;
-                v.x = __funnelshift_r(w[0], w[1], sh);
-                v.y = __funnelshift_r(w[1], w[2], sh);
-                v.z = __funnelshift_r(w[2], w[3], sh);
-                v.w = __funnelshift_r(w[3], w[4], sh);
-                *reinterpret_cast<uint4 *>(a.out + c) = v;
-            } else {
-                for (int q = 0; q < 16; q++) {
-                    const unsigned long long g = c + q;
-                    if (g >= g0 && g < g1) a.out[g] = stage[g - g0];
-                }
-            }
-        }
+        window_out(a.out, stage, base + W, base + wend, lane);
         __syncwarp();
+        ja = jb;
     }
 }
 
