@@ -79,7 +79,13 @@ bool plan_batch(const std::vector<double> &d_est, double safety, double target, 
 }
 
 // One pass over a group of jobs with the same k, all with readid text on the device.
+gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs);
+
 gx_status run_group(gx_ctx *c, const std::vector<gx_job *> &jobs) {
+    return guarded("gx_batch_run", [&] { return run_group_impl(c, jobs); });
+}
+
+gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
     cudaStream_t s = c->stream;
     const uint32_t n = (uint32_t)jobs.size();
     const int k = jobs[0]->k, wide = jobs[0]->wide;
@@ -439,7 +445,13 @@ void run_group_or_split(gx_ctx *c, const std::vector<gx_job *> &jobs, std::map<g
 
 }  // namespace
 
+static gx_status batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses);
+
 extern "C" gx_status gx_batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses) {
+    return guarded("gx_batch_run", [&] { return batch_run(c, jobs, n, statuses); });
+}
+
+static gx_status batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses) {
     if (!c || (!jobs && n) || n < 0) return GX_EINVAL;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaSetDevice(c->device);

@@ -116,10 +116,7 @@ void gx_ctx_destroy(gx_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    for (auto &e : c->marks)
-        if (e) cudaEventDestroy(e);
-    cudaStreamDestroy(c->stream);
-    delete c;
+    ctx_release(c);
 }
 
 gx_status gx_ctx_mark(gx_ctx *c, int slot) {
@@ -146,7 +143,13 @@ gx_status gx_ctx_synchronize(gx_ctx *c) {
     return GX_OK;
 }
 
+static gx_status job_create_impl(gx_ctx *c, const gx_job_opts *opts, gx_job **out);
+
 gx_status gx_job_create(gx_ctx *c, const gx_job_opts *opts, gx_job **out) {
+    return guarded("gx_job_create", [&] { return job_create_impl(c, opts, out); });
+}
+
+static gx_status job_create_impl(gx_ctx *c, const gx_job_opts *opts, gx_job **out) {
     if (!c || !opts || !out) return GX_EINVAL;
     *out = nullptr;
     if (opts->kmer_length < 3 || opts->kmer_length > 64) return GX_EINVAL;
@@ -156,6 +159,7 @@ gx_status gx_job_create(gx_ctx *c, const gx_job_opts *opts, gx_job **out) {
     gx_job *j = new (std::nothrow) gx_job();
     if (!j) return GX_ENOMEM;
     j->ctx = c;
+    c->refs.fetch_add(1);
     j->o = *opts;
     if (j->o.out_parts == 0) j->o.out_parts = 1;
     j->k = opts->kmer_length;
@@ -166,7 +170,13 @@ gx_status gx_job_create(gx_ctx *c, const gx_job_opts *opts, gx_job **out) {
     return GX_OK;
 }
 
+static gx_status job_add_input_impl(gx_job *j, const void *host, size_t bytes, int mate_stream);
+
 gx_status gx_job_add_input(gx_job *j, const void *host, size_t bytes, int mate_stream) {
+    return guarded("gx_job_add_input", [&] { return job_add_input_impl(j, host, bytes, mate_stream); });
+}
+
+static gx_status job_add_input_impl(gx_job *j, const void *host, size_t bytes, int mate_stream) {
     if (!j || (!host && bytes)) return GX_EINVAL;
     if (j->state != JS_INPUT) return GX_ESTATE;
     std::lock_guard<std::mutex> lk(j->ctx->mu);
@@ -225,7 +235,7 @@ gx_status gx_job_run(gx_job *j) {
     if (j->state != JS_INPUT) return GX_ESTATE;
     std::lock_guard<std::mutex> lk(j->ctx->mu);
     cudaSetDevice(j->ctx->device);
-    return run_job_locked(j);
+    return run_job_locked(j);  // exception-safe
 }
 
 gx_status gx_job_stats(const gx_job *j, gx_stats *out) {
@@ -243,7 +253,13 @@ gx_status gx_job_records_device(gx_job *j, const void **dev, size_t *bytes, cons
     return GX_OK;
 }
 
+static gx_status job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *written, int *more);
+
 gx_status gx_job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *written, int *more) {
+    return guarded("gx_job_emit", [&] { return job_emit(j, part, host_out, cap, written, more); });
+}
+
+static gx_status job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *written, int *more) {
     if (!j || !written || !more || (!host_out && cap)) return GX_EINVAL;
     if (j->state != JS_RAN) return GX_ESTATE;
     if (part < 0 || part >= j->o.out_parts) return GX_EINVAL;
@@ -269,7 +285,7 @@ gx_status gx_job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *w
         if (b > cur) {
             stop = b;
         } else {
-            CK(cudaMemcpy(host_out, j->d_out + cur, cap, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(host_out, j->d_out + cur, std::min<uint64_t>(cap, end - cur), cudaMemcpyDeviceToHost));
             const uint8_t *h = (const uint8_t *)host_out;
             uint64_t p = 0;
             while (p + 8 <= cap) {
@@ -317,7 +333,9 @@ void gx_job_destroy(gx_job *j) {
         cudaStreamSynchronize(s);
         j->tm.destroy();
     }
+    gx_ctx *c = j->ctx;
     delete j;
+    ctx_release(c);
 }
 
 }  // extern "C"
@@ -824,9 +842,19 @@ static gx_status run_job(gx_job *j) {
     return partitioned ? build_partitioned(rc) : build_table(rc);
 }
 
+void gxi::ctx_release(gx_ctx *c) {
+    if (c->refs.fetch_sub(1) != 1) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto &e : c->marks)
+        if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
+
 gx_status gxi::run_job_locked(gx_job *j) {
     const uint64_t l0 = launches_this_thread();
-    gx_status st = run_job(j);
+    gx_status st = guarded("gx_job_run", [&] { return run_job(j); });
     j->st.kernel_launches = launches_this_thread() - l0;
     j->state = st == GX_OK ? JS_RAN : JS_FAILED;
     if (j->text_borrowed) {

@@ -2,8 +2,11 @@
 // (gx_job.cu) and the batched and served builds (gx_batch.cu, gx_serve.cu).
 #pragma once
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
+#include <exception>
 #include <memory>
+#include <new>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -42,6 +45,9 @@ struct gx_ctx {
     std::mutex mu;
     size_t mem_limit = 0;
     cudaEvent_t marks[16] = {};
+    // the handle holds one reference and every job one more: a context destroyed while jobs
+    // still live is freed with the last of them
+    std::atomic<int> refs{1};
 };
 
 struct gx_job {
@@ -107,6 +113,27 @@ struct RunArena {
     }
     ~RunArena() { release(); }
 };
+
+// No C++ exception may cross the C ABI: a host allocation failure becomes GX_ENOMEM,
+// anything else GX_ECUDA, with the reason on stderr.
+template <class F>
+gx_status guarded(const char *where, F &&f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc &) {
+        fprintf(stderr, "gxgpu: %s: out of host memory\n", where);
+        return GX_ENOMEM;
+    } catch (const std::exception &e) {
+        fprintf(stderr, "gxgpu: %s: %s\n", where, e.what());
+        return GX_ECUDA;
+    } catch (...) {
+        fprintf(stderr, "gxgpu: %s: unexpected exception\n", where);
+        return GX_ECUDA;
+    }
+}
+
+// Drops one reference to a context; the last one frees it.
+void ctx_release(gx_ctx *c);
 
 // Runs one job; the caller holds the context's lock and has made its device current.
 gx_status run_job_locked(gx_job *j);

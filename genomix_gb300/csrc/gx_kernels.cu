@@ -262,6 +262,59 @@ __device__ bool java_parse_long(const uint8_t *s, uint32_t n, long long &out) {
     return true;
 }
 
+// SWAR byte classes of one 32-bit word of text (4 bytes, first in the low byte): bit q of the
+// result is byte q's flag.
+__device__ __forceinline__ uint32_t zero_bytes(uint32_t t) {  // high bit of every zero byte, exact
+    return ~(((t & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | t) & 0x80808080u;
+}
+__device__ __forceinline__ uint32_t high_bits_to_mask4(uint32_t z) {
+    return (((z >> 7) & 0x01010101u) * 0x01020408u) >> 24;
+}
+// tab bytes, and bytes outside [ACGTacgt]
+__device__ __forceinline__ void classify_word(uint32_t w, uint32_t &tab4, uint32_t &bad4) {
+    tab4 = high_bits_to_mask4(zero_bytes(w ^ 0x09090909u));
+    const uint32_t u = w & 0xDFDFDFDFu;
+    const uint32_t ok = zero_bytes(u ^ 0x41414141u) | zero_bytes(u ^ 0x43434343u) | zero_bytes(u ^ 0x47474747u) |
+                        zero_bytes(u ^ 0x54545454u);
+    bad4 = high_bits_to_mask4(~ok & 0x80808080u);
+}
+// bits [lo, hi) of a 32-bit mask (lo, hi clamped to [0, 32])
+__device__ __forceinline__ uint32_t bit_range(long long lo, long long hi) {
+    lo = lo < 0 ? 0 : (lo > 32 ? 32 : lo);
+    hi = hi < 0 ? 0 : (hi > 32 ? 32 : hi);
+    if (hi <= lo) return 0u;
+    const uint32_t top = hi >= 32 ? 0xffffffffu : ((1u << (uint32_t)hi) - 1u);
+    return top & ~((1u << (uint32_t)lo) - 1u);
+}
+
+constexpr int PARSE_SPAN = 32;                  // text bytes per lane per step
+constexpr int PARSE_STEP = 32 * PARSE_SPAN;     // bytes per warp step
+constexpr int PARSE_KEEP = 2;                   // steps whose letter masks stay in registers
+
+// tab and non-ACGT masks of the 32 bytes at `base` (16-byte aligned), limited to [b, e)
+__device__ __forceinline__ void classify_span(const uint8_t *text, uint64_t n_text, uint64_t base, uint64_t b,
+                                              uint64_t e, uint32_t &tm, uint32_t &nt, uint32_t &bm) {
+    tm = nt = bm = 0;
+    if (base >= e) return;
+    uint32_t tab = 0, bad = 0;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        uint32_t wd[4];
+        load16(text, n_text, base + 16 * h, wd);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            uint32_t t4, b4;
+            classify_word(wd[q], t4, b4);
+            tab |= t4 << (16 * h + 4 * q);
+            bad |= b4 << (16 * h + 4 * q);
+        }
+    }
+    const uint32_t im = bit_range((long long)b - (long long)base, (long long)e - (long long)base);
+    tm = tab & im;
+    nt = im & ~tm;
+    bm = bad & nt;
+}
+
 __global__ void __launch_bounds__(256) k_parse_lines(const uint8_t *text, uint64_t n_text,
                                                      const unsigned long long *line_end, uint32_t n_lines, int k,
                                                      LineRec *lines, uint8_t *lflags, uint32_t *nvalid,
@@ -275,29 +328,19 @@ __global__ void __launch_bounds__(256) k_parse_lines(const uint8_t *text, uint64
         if (e < n_text && e > b && text[e] == '\n' && text[e - 1] == '\r') e--;
         const uint32_t len = (uint32_t)(e - b);
 
-        // pass 1: tabs (first three positions, total) and the last non-tab byte
+        // one pass: tab positions (the first three, and how many), the last non-tab byte,
+        // and the bytes outside [ACGTacgt] (kept for the first PARSE_KEEP steps)
         uint32_t tab[3] = {len, len, len};
         uint32_t found = 0, tabs = 0;
         int last_nt = -1;
+        uint32_t keep_bm[PARSE_KEEP] = {0u, 0u};
         const uint64_t c0 = b & ~15ULL;
-        for (uint64_t w = c0; w < e; w += 512) {
-            const uint64_t chunk = w + 16 * (uint64_t)lane;
-            uint32_t tm = 0;
-            int lnt = -1;
-            if (chunk < e) {
-                uint32_t wd[4];
-                load16(text, n_text, chunk, wd);
-#pragma unroll
-                for (int q = 0; q < 16; q++) {
-                    const uint64_t p = chunk + q;
-                    if (p < b || p >= e) continue;
-                    const uint32_t c = (wd[q >> 2] >> (8 * (q & 3))) & 0xffu;
-                    if (c == '\t')
-                        tm |= 1u << q;
-                    else
-                        lnt = (int)(p - b);
-                }
-            }
+        uint32_t step = 0;
+        for (uint64_t w = c0; w < e; w += PARSE_STEP, step++) {
+            const uint64_t base = w + (uint64_t)PARSE_SPAN * lane;
+            uint32_t tm, nt, bm;
+            classify_span(text, n_text, base, b, e, tm, nt, bm);
+            if (step < PARSE_KEEP) keep_bm[step] = bm;
             const uint32_t cl = __popc(tm);
             const uint32_t incl = warp_inclusive_scan(cl);
             const uint32_t pre = incl - cl;
@@ -310,12 +353,13 @@ __global__ void __launch_bounds__(256) k_parse_lines(const uint8_t *text, uint64
                 if (own) {
                     uint32_t m = tm;
                     for (uint32_t i = 0; i < rr - pre; i++) m &= m - 1;
-                    pos = (uint32_t)(chunk + (__ffs(m) - 1) - b);
+                    pos = (uint32_t)(base + (__ffs(m) - 1) - b);
                 }
                 tab[r] = __shfl_sync(0xffffffffu, pos, __ffs(om) - 1);
             }
             found = min(3u, found + wt);
             tabs += wt;
+            const int lnt = nt ? (int)(base + 31 - __clz(nt) - b) : -1;
             last_nt = max(last_nt, __reduce_max_sync(0xffffffffu, lnt));
         }
         // String.split: trailing empty fields removed; no tab at all gives one field
@@ -332,25 +376,22 @@ __global__ void __launch_bounds__(256) k_parse_lines(const uint8_t *text, uint64
         const uint32_t f2b = tab[1] + 1, f2e = tabs >= 3 ? tab[2] : len;
         bool bad1 = false, bad2 = false;
         if (nf == 2 || nf == 3) {
-            // pass 2: [ACGTacgt]+ over fields 1 and 2
-            const uint32_t vb = f1b, ve = nf == 3 ? f2e : f1e;
-            uint32_t lb1 = 0, lb2 = 0;
-            for (uint64_t w = (b + vb) & ~15ULL; w < b + ve; w += 512) {
-                const uint64_t chunk = w + 16 * (uint64_t)lane;
-                if (chunk < b + ve) {
-                    uint32_t wd[4];
-                    load16(text, n_text, chunk, wd);
-#pragma unroll
-                    for (int q = 0; q < 16; q++) {
-                        const uint64_t p = chunk + q;
-                        if (p < b + vb || p >= b + ve) continue;
-                        const uint32_t rel = (uint32_t)(p - b);
-                        const uint32_t c = (wd[q >> 2] >> (8 * (q & 3))) & 0xffu;
-                        const bool ok = is_acgt(c);
-                        if (rel >= f1b && rel < f1e && !ok) lb1 = 1;
-                        if (nf == 3 && rel >= f2b && rel < f2e && !ok) lb2 = 1;
-                    }
+            // [ACGTacgt]+ over fields 1 and 2, from the kept masks (a longer line reads the
+            // rest of its text again)
+            bool lb1 = false, lb2 = false;
+            step = 0;
+            for (uint64_t w = c0; w < e; w += PARSE_STEP, step++) {
+                const uint64_t base = w + (uint64_t)PARSE_SPAN * lane;
+                uint32_t bm;
+                if (step < PARSE_KEEP) {
+                    bm = keep_bm[step];
+                } else {
+                    uint32_t tm, nt;
+                    classify_span(text, n_text, base, b, e, tm, nt, bm);
                 }
+                const long long rel = (long long)base - (long long)b;
+                lb1 |= (bm & bit_range((long long)f1b - rel, (long long)f1e - rel)) != 0;
+                if (nf == 3) lb2 |= (bm & bit_range((long long)f2b - rel, (long long)f2e - rel)) != 0;
             }
             bad1 = __any_sync(0xffffffffu, lb1);
             bad2 = __any_sync(0xffffffffu, lb2);
@@ -1596,6 +1637,8 @@ void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const 
 }
 
 // ---- B1 -------------------------------------------------------------------------------------
+constexpr int FINE_PER_THREAD = CHUNK / 256;  // occurrences of a chunk per thread
+
 template <class K>
 __global__ void __launch_bounds__(256) k_fine_count(const K *okey, const ulonglong2 *chunks, const SuperInfo *sinfo,
                                                     unsigned long long *fine_cnt) {
@@ -1604,9 +1647,18 @@ __global__ void __launch_bounds__(256) k_fine_count(const K *okey, const ulonglo
     const uint32_t sp = (uint32_t)(ch.y >> 32), len = (uint32_t)ch.y;
     const SuperInfo si = sinfo[sp];
     for (uint32_t i = threadIdx.x; i < si.F; i += blockDim.x) bins[i] = 0;
+    // all of the thread's loads first, then the bins
+    K kk[FINE_PER_THREAD];
+#pragma unroll
+    for (int q = 0; q < FINE_PER_THREAD; q++) {
+        const uint32_t i = q * 256 + threadIdx.x;
+        kk[q] = i < len ? okey[ch.x + i] : (K)0;
+    }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x)
-        atomicAdd(&bins[fine_in_super(KeyOps<K>::hash(okey[ch.x + i]), si.log_s, si.F)], 1u);
+#pragma unroll
+    for (int q = 0; q < FINE_PER_THREAD; q++)
+        if (q * 256 + threadIdx.x < len)
+            atomicAdd(&bins[fine_in_super(KeyOps<K>::hash(kk[q]), si.log_s, si.F)], 1u);
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < si.F; i += blockDim.x)
         if (bins[i]) atomicAdd(&fine_cnt[si.fine_first + i], (unsigned long long)bins[i]);
@@ -1627,6 +1679,7 @@ template <class K>
 struct FineSmem {
     K key[CHUNK];
     uint16_t bits[CHUNK];
+    uint16_t bkt[CHUNK];
     uint32_t loff[MAX_FINE];
     uint32_t gbase[MAX_FINE];
     uint32_t cur[MAX_FINE];
@@ -1644,9 +1697,30 @@ __global__ void __launch_bounds__(256) k_scatter_fine(const K *okey, const uint1
     const SuperInfo si = sinfo[sp];
     const uint32_t f0 = si.fine_first, F = si.F, log_s = si.log_s;
     for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) sm.cur[i] = 0;
+    // the thread's occurrences stay in registers between the count and the placement
+    K kk[FINE_PER_THREAD];
+    uint32_t bk[FINE_PER_THREAD / 2];  // two fine-bucket indexes per word
+    uint32_t bb[FINE_PER_THREAD / 2];  // two edge-bit words per word
+#pragma unroll
+    for (int q = 0; q < FINE_PER_THREAD; q++) {
+        const uint32_t i = q * 256 + threadIdx.x;
+        kk[q] = i < len ? okey[ch.x + i] : (K)0;
+        const uint32_t bits = i < len ? (uint32_t)obits[ch.x + i] : 0u;
+        if (q & 1)
+            bb[q >> 1] |= bits << 16;
+        else
+            bb[q >> 1] = bits;
+    }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x)
-        atomicAdd(&sm.cur[fine_in_super(KeyOps<K>::hash(okey[ch.x + i]), log_s, F)], 1u);
+#pragma unroll
+    for (int q = 0; q < FINE_PER_THREAD; q++) {
+        const uint32_t bkt = fine_in_super(KeyOps<K>::hash(kk[q]), log_s, F);
+        if (q & 1)
+            bk[q >> 1] |= bkt << 16;
+        else
+            bk[q >> 1] = bkt;
+        if (q * 256 + threadIdx.x < len) atomicAdd(&sm.cur[bkt], 1u);
+    }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) {
         sm.loff[i] = sm.cur[i];
@@ -1656,19 +1730,20 @@ __global__ void __launch_bounds__(256) k_scatter_fine(const K *okey, const uint1
     block_scan_array(sm.loff, F, sm.ws);
     for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) sm.cur[i] = 0;
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
-        const K key = okey[ch.x + i];
-        const uint32_t b = fine_in_super(KeyOps<K>::hash(key), log_s, F);
-        const uint32_t pos = sm.loff[b] + atomicAdd(&sm.cur[b], 1u);
-        sm.key[pos] = key;
-        sm.bits[pos] = obits[ch.x + i];
+#pragma unroll
+    for (int q = 0; q < FINE_PER_THREAD; q++) {
+        if (q * 256 + threadIdx.x >= len) continue;
+        const uint32_t bkt = (bk[q >> 1] >> (16 * (q & 1))) & 0xffffu;
+        const uint32_t pos = sm.loff[bkt] + atomicAdd(&sm.cur[bkt], 1u);
+        sm.key[pos] = kk[q];
+        sm.bits[pos] = (uint16_t)(bb[q >> 1] >> (16 * (q & 1)));
+        sm.bkt[pos] = (uint16_t)bkt;
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
-        const K key = sm.key[i];
-        const uint32_t b = fine_in_super(KeyOps<K>::hash(key), log_s, F);
+        const uint32_t b = sm.bkt[i];
         const unsigned long long g = fine_off[f0 + b] + sm.gbase[b] + (i - sm.loff[b]);
-        okey2[g] = key;
+        okey2[g] = sm.key[i];
         obits2[g] = sm.bits[i];
     }
 }
@@ -1813,14 +1888,18 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
     const K *okey = (const K *)a.okey2 + o0;
     const uint16_t *obits = a.obits2 + o0;
     const uint32_t M = (uint32_t)(o1 - o0);
-    for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x) {
-        sm.key1[i] = 0;
-        sm.cnt[i] = 0;
-        sm.meta[i] = 0;
-        sm.nbytes[i] = 0;
-        sm.cu[i] = 0;
-        sm.cf[i] = 0;
-        sm.hstart[i] = 0xffffffffu;
+    {
+        const uint4 z = make_uint4(0, 0, 0, 0), ones = make_uint4(~0u, ~0u, ~0u, ~0u);
+        uint4 *k4 = reinterpret_cast<uint4 *>(sm.key1);
+        for (uint32_t i = threadIdx.x; i < AGG_SLOTS * sizeof(K) / 16; i += blockDim.x) k4[i] = z;
+        for (uint32_t i = threadIdx.x; i < AGG_SLOTS / 4; i += blockDim.x) {
+            reinterpret_cast<uint4 *>(sm.cnt)[i] = z;
+            reinterpret_cast<uint4 *>(sm.meta)[i] = z;
+            reinterpret_cast<uint4 *>(sm.nbytes)[i] = z;
+            reinterpret_cast<uint4 *>(sm.cu)[i] = z;
+            reinterpret_cast<uint4 *>(sm.cf)[i] = z;
+            reinterpret_cast<uint4 *>(sm.hstart)[i] = ones;
+        }
     }
     if (threadIdx.x == 0) {
         sm.n = 0;
@@ -1931,7 +2010,29 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
         hk[i] = head_sort_key(sm.rank_of_slot[h.slot], h.uuid);
     }
     __syncthreads();
-    bitonic_sort_pairs<unsigned long long, uint32_t>(hk, hv, hc);
+    if (hc <= blockDim.x) {
+        // few heads (the usual case): each thread places its own by counting the smaller
+        // (key, read) pairs; read ordinals are distinct, so the ranks are too
+        unsigned long long mk = 0;
+        uint32_t mv = 0, rank = 0;
+        if (threadIdx.x < hc) {
+            mk = hk[threadIdx.x];
+            mv = hv[threadIdx.x];
+            for (uint32_t j = 0; j < hc; j++) {
+                const unsigned long long kj = hk[j];
+                const uint32_t vj = hv[j];
+                rank += (kj < mk || (kj == mk && vj < mv)) ? 1u : 0u;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < hc) {
+            hk[rank] = mk;
+            hv[rank] = mv;
+        }
+        __syncthreads();
+    } else {
+        bitonic_sort_pairs<unsigned long long, uint32_t>(hk, hv, hc);
+    }
     if (threadIdx.x == 0) {
         sm.kept = 0;
         sm.carry = 0;

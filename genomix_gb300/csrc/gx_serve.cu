@@ -69,7 +69,20 @@ struct gx_server {
     gx_serve_stats stats{};
 };
 
+static void lane_loop_impl(gx_server *sv, gx_ctx *lane);
+
+// a lane thread must never end the process: report, fail what it holds, stop the lane
 static void lane_loop(gx_server *sv, gx_ctx *lane) {
+    try {
+        lane_loop_impl(sv, lane);
+    } catch (const std::exception &e) {
+        fprintf(stderr, "gxgpu: serving lane stopped: %s\n", e.what());
+    } catch (...) {
+        fprintf(stderr, "gxgpu: serving lane stopped: unexpected exception\n");
+    }
+}
+
+static void lane_loop_impl(gx_server *sv, gx_ctx *lane) {
     std::unique_lock<std::mutex> lk(sv->mu);
     for (;;) {
         // admit in arrival order while memory lasts
@@ -104,8 +117,8 @@ static void lane_loop(gx_server *sv, gx_ctx *lane) {
         sv->stats.batches++;
         if (take.size() > sv->stats.max_batch_jobs) sv->stats.max_batch_jobs = take.size();
         lk.unlock();
-        std::vector<gx_status> st(jobs.size(), GX_OK);
-        gx_batch_run(lane, jobs.data(), (int)jobs.size(), st.data());
+        std::vector<gx_status> st(jobs.size(), GX_ECUDA);
+        gx_batch_run(lane, jobs.data(), (int)jobs.size(), st.data());  // exception-safe
         const double t1 = now_ms();
         lk.lock();
         for (size_t q = 0; q < take.size(); q++) {
@@ -125,7 +138,13 @@ static void lane_loop(gx_server *sv, gx_ctx *lane) {
 
 extern "C" {
 
+static gx_status serve_create_impl(gx_ctx *ctx, const gx_serve_opts *opts, gx_server **out);
+
 gx_status gx_serve_create(gx_ctx *ctx, const gx_serve_opts *opts, gx_server **out) {
+    return guarded("gx_serve_create", [&] { return serve_create_impl(ctx, opts, out); });
+}
+
+static gx_status serve_create_impl(gx_ctx *ctx, const gx_serve_opts *opts, gx_server **out) {
     if (!ctx || !out) return GX_EINVAL;
     if (opts && opts->struct_size < sizeof(gx_serve_opts)) return GX_EINVAL;
     *out = nullptr;
@@ -151,7 +170,13 @@ gx_status gx_serve_create(gx_ctx *ctx, const gx_serve_opts *opts, gx_server **ou
     return GX_OK;
 }
 
+static gx_status serve_submit_impl(gx_server *sv, gx_job *j, uint64_t *ticket);
+
 gx_status gx_serve_submit(gx_server *sv, gx_job *j, uint64_t *ticket) {
+    return guarded("gx_serve_submit", [&] { return serve_submit_impl(sv, j, ticket); });
+}
+
+static gx_status serve_submit_impl(gx_server *sv, gx_job *j, uint64_t *ticket) {
     if (!sv || !j || !ticket) return GX_EINVAL;
     if (j->ctx->device != sv->device) return GX_EINVAL;
     if (j->state != JS_INPUT) return GX_ESTATE;
@@ -177,7 +202,15 @@ gx_status gx_serve_submit(gx_server *sv, gx_job *j, uint64_t *ticket) {
     return GX_OK;
 }
 
+static gx_status serve_poll_impl(gx_server *sv, uint64_t ticket, int timeout_ms, gx_status *job_status,
+                        double *latency_ms);
+
 gx_status gx_serve_poll(gx_server *sv, uint64_t ticket, int timeout_ms, gx_status *job_status,
+                        double *latency_ms) {
+    return guarded("gx_serve_poll", [&] { return serve_poll_impl(sv, ticket, timeout_ms, job_status, latency_ms); });
+}
+
+static gx_status serve_poll_impl(gx_server *sv, uint64_t ticket, int timeout_ms, gx_status *job_status,
                         double *latency_ms) {
     if (!sv) return GX_EINVAL;
     std::unique_lock<std::mutex> lk(sv->mu);

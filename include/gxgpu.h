@@ -128,6 +128,8 @@ typedef struct gx_stats {
 /* Create a context on CUDA device `device`.  opts may be NULL.  Replaces the connection to
  * the Hyracks cluster controller made in GenomixHyracksDriver.java:70-78. */
 gx_status gx_ctx_create(int device, const gx_ctx_opts *opts, gx_ctx **out);
+/* Jobs created on a context keep it alive: after gx_ctx_destroy they can still run, emit and
+ * be destroyed, and the context goes with the last of them. */
 void gx_ctx_destroy(gx_ctx *ctx);
 
 /* Device-side timing on the context's stream: gx_ctx_mark records event `slot` (0..15),

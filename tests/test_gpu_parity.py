@@ -243,3 +243,15 @@ def test_seqfile_of_gpu_records(ctx):
     text = synth.small_random(51, 300, 100, 21, paired=True)
     rec, _ = gpu_build(ctx, text, 21)
     assert gx.seqfile_read(gx.seqfile_write(rec, seed=1)) == rec
+
+
+def test_job_outlives_its_context():
+    text = synth.small_random(77, 200, 80, 21)
+    c = gx.Context(0)
+    job = gx.GraphBuildJob(c, 21)
+    job.add_input(text)
+    c.close()  # the job keeps the context alive
+    job.run()
+    rec = job.records()
+    job.close()
+    assert go.normalize(rec) == go.normalize(go.build_graph(text, 21).records)
