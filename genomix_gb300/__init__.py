@@ -14,6 +14,7 @@ from .graph import (
     batch_run,
     fastq_to_readid,
     iter_records,
+    records_digest,
     records_to_text,
     seqfile_read,
     seqfile_write,
@@ -21,5 +22,5 @@ from .graph import (
 
 __all__ = [
     "Context", "GenomixGpuDriver", "GraphBuildError", "GraphBuildJob", "PinnedBuffer", "Server", "batch_run",
-    "fastq_to_readid", "iter_records", "records_to_text", "seqfile_read", "seqfile_write",
+    "fastq_to_readid", "iter_records", "records_digest", "records_to_text", "seqfile_read", "seqfile_write",
 ]

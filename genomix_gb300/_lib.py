@@ -27,6 +27,7 @@ EXPORTS = [
     "gx_pinned_free", "gx_fastq_to_readid", "gx_host_free", "gx_seqfile_write", "gx_seqfile_read",
     "gx_records_to_text", "gx_build_noalloc",
     "gx_serve_create", "gx_serve_submit", "gx_serve_poll", "gx_serve_stats_get", "gx_serve_destroy",
+    "gx_records_digest",
 ]
 
 
@@ -57,6 +58,13 @@ class ServeOpts(ctypes.Structure):
 class ServeStats(ctypes.Structure):
     _fields_ = [(f, ctypes.c_uint64) for f in ("jobs_submitted", "jobs_done", "batches", "max_batch_jobs",
                                                 "jobs_waiting", "jobs_running", "bytes_in_use")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Digest(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("records", "edges", "heads", "coverage", "sum", "xor_")]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -120,6 +128,7 @@ def load():
         "gx_serve_poll": ([vp, ctypes.c_uint64, i, P(i), P(ctypes.c_double)], i),
         "gx_serve_stats_get": ([vp, P(ServeStats)], i),
         "gx_serve_destroy": ([vp], None),
+        "gx_records_digest": ([vp, sz, P(Digest)], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -3,12 +3,14 @@
 //   - FASTQ -> readid conversion (GenomixDriver.convertAndUploadFastqToHDFS, :665-714)
 //   - Hadoop 0.20.2 SequenceFile container (KmerNodePairSequenceWriterFactory.java:66-73)
 //   - text dump of records (GenomixClusterManager.copyBinAndTextToLocal, :371)
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gxgpu.h"
@@ -289,6 +291,127 @@ static void read_head_set_text(Cur &c, std::string &o) {
     o.push_back(']');
 }
 
+// ---- order-independent digest of a record stream ----------------------------------------
+static inline uint64_t mix64(uint64_t z) {  // SplitMix64 finaliser
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+static inline uint64_t hash_bytes(uint64_t h, const uint8_t *s, size_t n) {  // FNV-1a, 64-bit
+    for (size_t i = 0; i < n; i++) h = (h ^ s[i]) * 0x100000001B3ULL;
+    return h;
+}
+
+static gx_status digest_range(const uint8_t *rec, size_t n, gx_digest &d);
+
+// Every record hashed in its normal form (each edge list's elements in byte order; read-head
+// sets as written, since their order is the TreeSet's), the hashes combined by sum and xor.
+// Large streams are cut at record boundaries and digested on all host threads.
+gx_status records_digest(const uint8_t *rec, size_t n, gx_digest &d) {
+    memset(&d, 0, sizeof d);
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    if (n < (64u << 20) || hw == 1) return digest_range(rec, n, d);
+    std::vector<size_t> cut{0};
+    const size_t step = n / hw;
+    size_t p = 0, next = step;
+    while (p < n) {
+        if (n - p < 8) return GX_EINVAL;
+        const uint64_t rl = rd32(rec + p);
+        if (rl + 8 > n - p) return GX_EINVAL;
+        p += 8 + rl;
+        if (p >= next && p < n) {
+            cut.push_back(p);
+            next = p + step;
+        }
+    }
+    cut.push_back(n);
+    const size_t T = cut.size() - 1;
+    std::vector<gx_digest> part(T);
+    std::vector<gx_status> st(T, GX_OK);
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < T; t++)
+        th.emplace_back([&, t] { st[t] = digest_range(rec + cut[t], cut[t + 1] - cut[t], part[t]); });
+    for (auto &x : th) x.join();
+    for (size_t t = 0; t < T; t++) {
+        if (st[t] != GX_OK) return st[t];
+        d.records += part[t].records;
+        d.edges += part[t].edges;
+        d.heads += part[t].heads;
+        d.coverage += part[t].coverage;
+        d.sum += part[t].sum;
+        d.xor_ ^= part[t].xor_;
+    }
+    return GX_OK;
+}
+
+static gx_status digest_range(const uint8_t *rec, size_t n, gx_digest &d) {
+    memset(&d, 0, sizeof d);
+    size_t p = 0;
+    std::vector<const uint8_t *> el;
+    while (p < n) {
+        if (n - p < 8) return GX_EINVAL;
+        const uint32_t rl = rd32(rec + p), kl = rd32(rec + p + 4);
+        if ((uint64_t)rl + 8 > n - p || kl > rl || kl < 4) return GX_EINVAL;
+        const uint8_t *r = rec + p + 8, *re = r + rl;
+        uint64_t h = hash_bytes(0xCBF29CE484222325ULL, r, kl);  // the key
+        Cur c{r + kl, re};
+        const uint8_t active = c.u8();
+        h = hash_bytes(h, &active, 1);
+        for (int t = 0; t < 4; t++) {
+            if (!(active & (1 << t))) continue;
+            const uint32_t cnt = c.u32();
+            el.clear();
+            size_t esz = 0;
+            for (uint32_t i = 0; i < cnt && c.ok; i++) {
+                if (!c.need(4)) break;
+                const uint32_t kk = rd32(c.p);
+                esz = 4 + (kk + 3) / 4;
+                if (!c.need(esz)) break;
+                el.push_back(c.p);
+                c.p += esz;
+            }
+            if (!c.ok) return GX_EINVAL;
+            std::sort(el.begin(), el.end(),
+                      [esz](const uint8_t *a, const uint8_t *b) { return memcmp(a, b, esz) < 0; });
+            const uint8_t tb = (uint8_t)t;
+            h = hash_bytes(h, &tb, 1);
+            for (const uint8_t *e : el) h = hash_bytes(h, e, esz);
+            d.edges += cnt;
+        }
+        for (int set = 0; set < 2; set++) {
+            if (!(active & (0x10 << set))) continue;
+            const uint8_t *s0 = c.p;
+            if (c.u8() != 1) return GX_EINVAL;
+            const uint32_t cnt = c.u32();
+            for (uint32_t i = 0; i < cnt && c.ok; i++) {
+                const uint8_t flags = c.u8();
+                if (!c.need(8)) return GX_EINVAL;
+                c.p += 8;
+                for (int m = 0; m < ((flags & 1) ? 2 : 1) && c.ok; m++) {
+                    const uint32_t L = c.u32();
+                    if (c.need((L + 3) / 4)) c.p += (L + 3) / 4;
+                }
+            }
+            if (!c.ok) return GX_EINVAL;
+            h = hash_bytes(h, s0, (size_t)(c.p - s0));
+            d.heads += cnt;
+        }
+        if (!(active & 0x80) || !c.need(4) || c.p + 4 != re) return GX_EINVAL;
+        const uint32_t cb = rd32(c.p);
+        float cov;
+        memcpy(&cov, &cb, 4);
+        d.coverage += (uint64_t)cov;
+        h = hash_bytes(h, c.p, 4);
+        h = mix64(h);
+        d.records++;
+        d.sum += h;
+        d.xor_ ^= h;
+        p += 8 + rl;
+    }
+    return GX_OK;
+}
+
 gx_status records_to_text(const uint8_t *rec, size_t n, std::string &o) {
     static const char *ET[4] = {"FF", "FR", "RF", "RR"};
     size_t p = 0;
@@ -415,6 +538,15 @@ gx_status gx_seqfile_read(const void *file, size_t bytes, uint8_t **out, size_t 
     gx_status st = gxh::seqfile_read((const uint8_t *)file, bytes, o);
     if (st != GX_OK) return st;
     return give(o, (void **)out, out_bytes);
+}
+
+gx_status gx_records_digest(const void *records, size_t bytes, gx_digest *out) {
+    if ((!records && bytes) || !out) return GX_EINVAL;
+    try {
+        return gxh::records_digest((const uint8_t *)records, bytes, *out);
+    } catch (...) {
+        return GX_ENOMEM;
+    }
 }
 
 gx_status gx_records_to_text(const void *records, size_t bytes, char **out, size_t *out_bytes) {

@@ -15,4 +15,5 @@ gx_status fastq_to_readid(const uint8_t *m1, size_t n1, const uint8_t *m2, size_
 gx_status seqfile_write(const uint8_t *rec, size_t n, const uint8_t *sync, uint64_t seed, std::string &out);
 gx_status seqfile_read(const uint8_t *f, size_t n, std::string &out);
 gx_status records_to_text(const uint8_t *rec, size_t n, std::string &out);
+gx_status records_digest(const uint8_t *rec, size_t n, gx_digest &d);
 }  // namespace gxh

@@ -189,6 +189,10 @@ class GraphBuildJob:
         _check(self._L.gx_job_emit(self.h, part, buf_ptr, cap, ctypes.byref(w), ctypes.byref(m)), "gx_job_emit")
         return w.value, bool(m.value)
 
+    def rewind(self, part=None):
+        """Restarts gx_job_emit at the beginning of one part (or of every part)."""
+        _check(self._L.gx_job_emit_rewind(self.h, -1 if part is None else part), "gx_job_emit_rewind")
+
     def records(self, part=None, chunk=None):
         """Serialized record stream of one part (or all parts in order) as bytes."""
         parts = range(self.out_parts) if part is None else [part]
@@ -331,6 +335,20 @@ def records_to_text(records: bytes) -> str:
     st, out = _buf_out(L.gx_records_to_text, records, len(records))
     _check(st, "gx_records_to_text")
     return out.decode()
+
+
+def records_digest(records, nbytes=None):
+    """Order-independent digest of a record stream (host bytes, or a host pointer + size)."""
+    L = _lib.load()
+    d = _lib.Digest()
+    if isinstance(records, int):
+        p, n = records, nbytes
+        _check(L.gx_records_digest(p, n, ctypes.byref(d)), "gx_records_digest")
+    else:
+        p, n, keep = _host_ptr(records)
+        _check(L.gx_records_digest(p, n, ctypes.byref(d)), "gx_records_digest")
+        del keep
+    return d.as_dict()
 
 
 def iter_records(records: bytes):

@@ -187,13 +187,41 @@ def _err_ramp(L=250):
     return 0.002 + 0.013 * (pos - 1) / (L - 1)
 
 
-def pe_50mbp(max_pairs=None, genome_len=50_000_000):
-    rng = rng_for(3)
-    g = random_genome(rng, genome_len, 0.41)
-    plant_repeats(rng, g, 300, 20, 0.05 * genome_len)
+_GENOMES = {}
+
+
+def _pe50_genome(genome_len):
+    """The 50 Mbp genome at GC 41% with 5% of its length in 300 bp units repeated 20 times."""
+    if genome_len not in _GENOMES:
+        rng = rng_for(3)
+        g = random_genome(rng, genome_len, 0.41)
+        plant_repeats(rng, g, 300, 20, 0.05 * genome_len)
+        _GENOMES[genome_len] = g
+    return _GENOMES[genome_len]
+
+
+def _pe50_chunk(c, n, genome_len):
+    """Pairs [c * CHUNK, c * CHUNK + n) of the long-k workload, from their own seed."""
+    g = _pe50_genome(genome_len)
+    rng = np.random.Generator(np.random.PCG64(np.random.SeedSequence([SEED_BASE + 3000, c])))
+    mates = simulate_chunk(rng, g, n, 250, True, 600, 60, _err_ramp(250), 0.0)
+    return readid_lines(c * CHUNK, mates).tobytes()
+
+
+def pe_50mbp(max_pairs=None, genome_len=50_000_000, pool=None):
+    """2 x 250 bp pairs at 20x, insert N(600, 60), substitutions rising from 0.2% to 1.5% along
+    the read, k = 55.  Every CHUNK of pairs has its own seed, so `pool` (an executor) can
+    generate the chunks in parallel with the same result."""
     pairs = int(round(20 * genome_len / 500))
-    text, n = _build(rng, g, pairs, 250, True, 600, 60, _err_ramp(250), 0.0, max_pairs)
-    return Workload("pe_50mbp_2x250_k55", 55, text, n, True, len(g))
+    n = pairs if max_pairs is None else min(pairs, int(max_pairs))
+    nch = (n + CHUNK - 1) // CHUNK
+    cs = list(range(nch))
+    ns = [min(CHUNK, n - c * CHUNK) for c in cs]
+    if pool is None:
+        parts = [_pe50_chunk(c, m, genome_len) for c, m in zip(cs, ns)]
+    else:
+        parts = list(pool.map(_pe50_chunk, cs, ns, [genome_len] * nch))
+    return Workload("pe_50mbp_2x250_k55", 55, b"".join(parts), n, True, genome_len)
 
 
 def batched_sample(s, scale=1.0):

@@ -290,6 +290,18 @@ gx_status gx_seqfile_write(const void *records, size_t bytes, const uint8_t *syn
  * (uncompressed).  *out is malloc'ed. */
 gx_status gx_seqfile_read(const void *file, size_t bytes, uint8_t **out, size_t *out_bytes);
 
+/* Order-independent digest of a record stream: every record hashed in its normal form
+ * (each edge list's elements in byte order, read-head sets in their TreeSet order), the
+ * hashes combined by sum and by xor; with counts of records, edges, read heads and the
+ * coverage total.  Two streams hold the same Node set exactly when their digests agree
+ * (up to hash collisions).  A verification helper with no counterpart in the reference (its
+ * tests compare sorted text dumps, TestUtils.java:67-181). */
+typedef struct gx_digest {
+    uint64_t records, edges, heads, coverage;
+    uint64_t sum, xor_;
+} gx_digest;
+gx_status gx_records_digest(const void *records, size_t bytes, gx_digest *out);
+
 /* Text dump of a record stream, one line per record in the form
  * key.toString() + "\t" + value.toString() that GenomixClusterManager.copyBinAndTextToLocal
  * writes (GenomixClusterManager.java:371; Node.toString Node.java:524-537).  *out is malloc'ed. */

@@ -77,3 +77,23 @@ def test_seqfile_round_trip_and_header():
         res.records) // 2200
     assert gx.seqfile_write(res.records, seed=5) == f  # deterministic sync marker
     assert gx.seqfile_write(res.records, seed=6) != f
+
+
+def test_records_digest_is_order_independent_and_counts():
+    from conftest import golden_input
+    text = golden_input("Random100_k3")
+    ref = go.build_graph(text, 3, threads=2, parts=3)
+    d = gx.records_digest(ref.records)
+    assert d["records"] == ref.nodes and d["heads"] == ref.read_heads and d["coverage"] == ref.kmers
+    recs = [(len(k) + len(v)).to_bytes(4, "big") + len(k).to_bytes(4, "big") + k + v
+            for k, v in gx.iter_records(ref.records)]
+    assert b"".join(recs) == ref.records
+    assert gx.records_digest(b"".join(reversed(recs))) == d
+    # another thread/part split of the oracle orders records differently: same digest
+    assert gx.records_digest(go.build_graph(text, 3, threads=1, parts=1).records) == d
+    # one changed byte (the last coverage byte of the first record) changes the digest
+    bad = bytearray(ref.records)
+    first_len = int.from_bytes(bad[0:4], "big") + 8
+    bad[first_len - 1] ^= 1
+    d2 = gx.records_digest(bytes(bad))
+    assert (d2["sum"], d2["xor_"]) != (d["sum"], d["xor_"])
