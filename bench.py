@@ -22,6 +22,9 @@ reads, see genomix_gb300/synth.py).
              the first pairs of the same workload, all host threads
   batched    the 64-sample workload (genomes log-uniform 20 kbp - 2 Mbp, 10-60x single-end
              150 bp, k = 31) built one gx_job_run per sample and as one gx_batch_run pass
+  long_k     the 50 Mbp workload (2 x 250 bp pairs at 20x, k = 55, 128-bit keys), plain build
+  autotune   the autotuner's choice (algorithm x table fill) on a prefix of the workload,
+             used by the timed builds; every candidate's time
   serving    a Poisson stream of jobs (genomes log-uniform 10 kbp - 5 Mbp, 30x, 2 x 150 bp
              pairs, k in {21, 31, 55}) through gx_serve_*, offered rate swept: p50/p99
              latency from arrival to completion and k-mers/s per rate
@@ -45,6 +48,7 @@ METRIC = "k-mers/s, bit-exact graph build, batched vs per-job, 1 GB300; p99 job 
 UNIT = "k-mers/s"
 CPU_SAMPLE_PAIRS = 120_000   # cpu_baseline sample (one run)
 REF_STEP_PAIRS = 60_000      # --impl reference: sample per step
+TUNE_PAIRS = 200_000         # autotuner sample: the first pairs of the workload
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_emit_write_part_pe5mbp_k31.md")
 HEADOUT_BYTES = 48           # one HeadOut entry (uuid, two text offsets, position, counts)
 
@@ -214,6 +218,15 @@ def bench_serving(ctx, works, rates=SERVE_RATES, n_req=SERVE_REQUESTS):
         pins.append(p)
     out = []
     with gx.Server(ctx) as srv:
+        # warm the lanes (first passes grow the memory pool), untimed
+        warm = []
+        for q in range(min(8, len(works))):
+            j = gx.GraphBuildJob(ctx, works[q].k)
+            j.add_input(pins[q])
+            warm.append((j, srv.submit(j)))
+        for j, t in warm:
+            assert srv.poll(t)[0] == 0
+            j.close()
         for rate in rates:
             arr = synth.poisson_arrivals(n_req, rate, seed_sample=1)
             tickets, jobs, t_sub = [None] * n_req, [None] * n_req, [0.0] * n_req
@@ -261,6 +274,47 @@ def bench_serving(ctx, works, rates=SERVE_RATES, n_req=SERVE_REQUESTS):
     return {"workload": "serving_pe150_30x_k21_31_55", "job_pool": len(works),
             "mean_job_bytes": sum(len(w.text) for w in works) / len(works), "rates": out,
             "highest_sustained": top, "passes": st["batches"], "max_jobs_per_pass": st["max_batch_jobs"]}
+
+
+def long_k_workload():
+    """The 50 Mbp, 2 x 250 bp, k = 55 workload, generated in a spawn pool (before any CUDA call)."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    from genomix_gb300 import synth
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as ex:
+        return synth.pe_50mbp(pool=ex)
+
+
+def bench_long_k(ctx, w, steps, warmup, local, autotune=True):
+    """The plain build of the long-k workload (128-bit keys), text resident in HBM."""
+    import torch
+    import genomix_gb300 as gx
+    tune = ctx.autotune(sample_prefix(w.text, 50_000), w.k) if autotune else None
+    d = torch.frombuffer(bytearray(w.text), dtype=torch.uint8).to(f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def step():
+        job = gx.GraphBuildJob(ctx, w.k)
+        job.add_input_device(d.data_ptr(), d.numel())
+        job.run()
+        st = job.stats()
+        job.close()
+        return st
+
+    for _ in range(warmup):
+        step()
+    ctx.mark(8)
+    sts = [step() for _ in range(steps)]
+    ctx.mark(9)
+    ms = ctx.elapsed_ms(8, 9) / steps
+    st = sts[0]
+    del d
+    return {"workload": w.name, "genome_bp": w.genome_len, "pairs": w.reads, "k": w.k, "key_bits": st["key_bits"],
+            "kmers": st["kmers"], "nodes": st["nodes"], "record_bytes": st["record_bytes"],
+            "kmers_per_s": st["kmers"] / (ms / 1e3), "ms_per_build": ms,
+            "phases_ms": {"parse": st["ms_parse"], "partition": st["ms_insert"], "aggregate": st["ms_aggregate"],
+                          "write": st["ms_write"]},
+            "autotune": tune}
 
 
 def bench_batched(ctx, samples, steps, warmup, local):
@@ -322,6 +376,7 @@ def bench_batched(ctx, samples, steps, warmup, local):
             "nodes": sum(st["nodes"] for st in ref),
             "plain_kmers_per_s": kmers / (ms_plain / 1e3), "batched_kmers_per_s": kmers / (ms_batched / 1e3),
             "speedup": ms_plain / ms_batched, "ms_plain": ms_plain, "ms_batched": ms_batched,
+            "buckets": sum(st["table_partitions"] for st in got), "passes": int(got[0]["attempts"]),
             "gpu_launches_plain": int(sum(st["kernel_launches"] for st in ref)),
             "gpu_launches_batched": int(got[0]["kernel_launches"]),
             "batched_phases_ms": {"parse": got[0]["ms_parse"], "partition": got[0]["ms_insert"],
@@ -369,8 +424,11 @@ def run_gb300(args, ws, rank, local):
     w = workload(args.max_pairs)
     samples = None if args.no_batched else batched_workload()
     serve_pool = None if args.no_serving else serving_workload()
+    w50 = None if args.no_long_k else long_k_workload()
     ctx = gx.Context(local)
     torch.cuda.set_device(local)
+    # the autotuner picks algorithm and fill on a prefix of the workload (untimed)
+    tune = None if args.no_autotune else ctx.autotune(sample_prefix(w.text, TUNE_PAIRS), w.k)
     d_text = torch.frombuffer(bytearray(w.text), dtype=torch.uint8).to(f"cuda:{local}")
     torch.cuda.synchronize()
 
@@ -429,6 +487,10 @@ def run_gb300(args, ws, rank, local):
         del samples
     if serve_pool is not None:
         srv = bench_serving(ctx, serve_pool)
+    lk = None
+    if w50 is not None:
+        lk = bench_long_k(ctx, w50, args.steps, args.warmup, local, autotune=not args.no_autotune)
+        del w50
 
     if rank != 0:
         return
@@ -467,8 +529,10 @@ def run_gb300(args, ws, rank, local):
                   "read_heads": stats[0]["read_heads"], "record_bytes": out_bytes,
                   "table_slots": stats[0]["table_slots"], "max_probe": stats[0]["max_probe"]},
         "clocks": clk.summary(),
+        "autotune": tune,
         "batched": bat,
         "serving": srv,
+        "long_k": lk,
         "cpu_baseline": cb,
     }
     print(json.dumps(line), flush=True)
@@ -486,6 +550,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-sample batched vs per-job measurement")
     ap.add_argument("--no-serving", action="store_true", help="skip the served-stream measurement")
+    ap.add_argument("--no-autotune", action="store_true", help="run with the built-in settings")
+    ap.add_argument("--no-long-k", action="store_true", help="skip the 50 Mbp k = 55 measurement")
     ap.add_argument("--max-pairs", type=int, default=None,
                     help="use only the first pairs of the workload (profiling captures)")
     args = ap.parse_args()

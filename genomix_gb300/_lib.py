@@ -27,7 +27,7 @@ EXPORTS = [
     "gx_pinned_free", "gx_fastq_to_readid", "gx_host_free", "gx_seqfile_write", "gx_seqfile_read",
     "gx_records_to_text", "gx_build_noalloc",
     "gx_serve_create", "gx_serve_submit", "gx_serve_poll", "gx_serve_stats_get", "gx_serve_destroy",
-    "gx_records_digest",
+    "gx_records_digest", "gx_autotune", "gx_autotune_clear",
 ]
 
 
@@ -63,6 +63,15 @@ class ServeStats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class TuneCand(ctypes.Structure):
+    _fields_ = [("algorithm", ctypes.c_int), ("load_factor", ctypes.c_double), ("ms", ctypes.c_double)]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("algorithm", ctypes.c_int), ("load_factor", ctypes.c_double),
+                ("ms", ctypes.c_double), ("tried", ctypes.c_int), ("cand", TuneCand * 16)]
+
+
 class Digest(ctypes.Structure):
     _fields_ = [(f, ctypes.c_uint64) for f in ("records", "edges", "heads", "coverage", "sum", "xor_")]
 
@@ -79,6 +88,7 @@ class Stats(ctypes.Structure):
         ("kernel_launches", ctypes.c_uint64),
         ("ms_parse", ctypes.c_double), ("ms_insert", ctypes.c_double), ("ms_emit", ctypes.c_double),
         ("ms_total", ctypes.c_double), ("ms_aggregate", ctypes.c_double), ("ms_write", ctypes.c_double),
+        ("attempts", ctypes.c_uint64),
     ]
 
     def as_dict(self):
@@ -129,6 +139,8 @@ def load():
         "gx_serve_stats_get": ([vp, P(ServeStats)], i),
         "gx_serve_destroy": ([vp], None),
         "gx_records_digest": ([vp, sz, P(Digest)], i),
+        "gx_autotune": ([vp, vp, sz, i, i, P(TuneResult)], i),
+        "gx_autotune_clear": ([vp], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -208,7 +208,7 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
     }
 
     double safety = 1.15;
-    const double target = (double)AGG_TARGET;
+    const double target = bucket_target(jobs[0]->eff_load_factor);  // one fill for the pass
     for (int attempt = 0;; attempt++) {
         std::vector<SamplePlan> plans;
         uint32_t S = 0, P = 0;
@@ -407,6 +407,7 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
             st.read_heads = nh;
             st.record_bytes = j->out_bytes;
             st.table_partitions = Pi;
+            st.attempts = (uint64_t)attempt + 1;
             st.table_slots = (uint64_t)Pi * AGG_SLOTS;
             st.cov_inexact_nodes = hs.cov_inexact;  // batch-wide
             st.kernel_launches = launches;         // the whole batch's launches
@@ -464,7 +465,8 @@ static gx_status batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses)
             result[j] = GX_ESTATE;
             continue;
         }
-        if (j->o.algorithm == GX_ALGO_TABLE) {
+        resolve_options(j);
+        if (j->eff_algorithm == GX_ALGO_TABLE) {
             result[j] = run_job_locked(j);
             continue;
         }
@@ -474,7 +476,7 @@ static gx_status batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses)
             result[j] = pe;
             continue;
         }
-        by_k[j->k].push_back(j);
+        by_k[j->k * 4096 + (int)(j->eff_load_factor * 1000)].push_back(j);  // same k and fill
         result[j] = GX_OK;  // placeholder until its group runs
     }
     for (auto &kv : by_k) {

@@ -402,7 +402,7 @@ static gx_status build_table(RunCtx &rc) {
     const int k = j->k;
     const uint32_t n_reads = rc.n_reads;
     const size_t slot_bytes = j->wide ? sizeof(Slot128) : sizeof(Slot64);
-    double lf = j->o.load_factor > 0 ? j->o.load_factor : 0.5;
+    double lf = j->eff_load_factor > 0 ? j->eff_load_factor : 0.5;
     DevStatus hs;
     for (int attempt = 0;; attempt++) {
         const uint64_t want = (uint64_t)((double)rc.n_occ / lf) + 1;
@@ -497,6 +497,7 @@ static gx_status build_table(RunCtx &rc) {
         if ((e = finish_outputs(rc, nparts, total, part_off, part_nodes, head_cnt2, outp)) != GX_OK) return e;
         j->st.table_slots = (uint64_t)nparts * PART_SLOTS;
         j->st.table_partitions = nparts;
+        j->st.attempts = (uint64_t)attempt + 1;
         j->st.max_probe = hs.max_probe;
         j->st.cov_inexact_nodes = hs.cov_inexact;
         j->st.ms_insert = tm.ms(2, 3);
@@ -522,7 +523,7 @@ static gx_status build_partitioned(RunCtx &rc) {
     double safety = 1.15;
     DevStatus hs;
     for (int attempt = 0;; attempt++) {
-        const double target = j->o.load_factor > 0 ? j->o.load_factor * AGG_SLOTS : (double)AGG_TARGET;
+        const double target = bucket_target(j->eff_load_factor);
         const PartPlan pp = plan_partitions(d_est, safety, target);
         const uint32_t S = 1u << pp.log_s, P = pp.P;
         // super counts at this resolution, offsets and CHUNK-sized pieces
@@ -708,6 +709,7 @@ static gx_status build_partitioned(RunCtx &rc) {
         if ((e = finish_outputs(rc, P, total, part_off, part_nodes, head_cnt2, outp)) != GX_OK) return e;
         j->st.table_slots = (uint64_t)P * AGG_SLOTS;
         j->st.table_partitions = P;
+        j->st.attempts = (uint64_t)attempt + 1;
         j->st.max_probe = 0;
         j->st.cov_inexact_nodes = hs.cov_inexact;
         j->st.ms_insert = tm.ms(2, 3);
@@ -752,7 +754,8 @@ static gx_status run_job(gx_job *j) {
     memset(&j->st, 0, sizeof j->st);
     j->st.key_bits = j->wide ? 128 : 64;
     const int k = j->k;
-    const bool partitioned = j->o.algorithm != GX_ALGO_TABLE;
+    resolve_options(j);
+    const bool partitioned = j->eff_algorithm != GX_ALGO_TABLE;
     {
         const gx_status pe = prepare_text(j);
         if (pe != GX_OK) return pe;
@@ -840,6 +843,20 @@ static gx_status run_job(gx_job *j) {
     rc.n_reads = n_reads;
     rc.n_occ = hs.n_occ;
     return partitioned ? build_partitioned(rc) : build_table(rc);
+}
+
+void gxi::resolve_options(gx_job *j) {
+    j->eff_algorithm = j->o.algorithm == GX_ALGO_TABLE ? GX_ALGO_TABLE : GX_ALGO_PARTITIONED;
+    j->eff_load_factor = j->o.load_factor;
+    const gx_ctx::Tuned &t = j->ctx->tuned[j->wide];
+    if (j->o.algorithm == GX_ALGO_DEFAULT && j->o.load_factor == 0 && t.valid) {
+        j->eff_algorithm = t.algorithm;
+        j->eff_load_factor = t.load_factor;
+    }
+}
+
+double gxi::bucket_target(double load_factor) {
+    return load_factor > 0 ? load_factor * AGG_SLOTS : (double)AGG_TARGET;
 }
 
 void gxi::ctx_release(gx_ctx *c) {

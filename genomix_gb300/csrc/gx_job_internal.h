@@ -48,6 +48,12 @@ struct gx_ctx {
     // the handle holds one reference and every job one more: a context destroyed while jobs
     // still live is freed with the last of them
     std::atomic<int> refs{1};
+    // gx_autotune's choice per key width (64- / 128-bit), used by jobs left at the defaults
+    struct Tuned {
+        bool valid = false;
+        int algorithm = GX_ALGO_PARTITIONED;
+        double load_factor = 0;
+    } tuned[2];
 };
 
 struct gx_job {
@@ -73,6 +79,9 @@ struct gx_job {
     std::vector<unsigned long long> h_part_off;  // lazily fetched copy of d_part_off
     gx_stats st{};
     gxi::Timers tm;
+    // the algorithm and fill this run uses: the job's options, or the context's tuned choice
+    int eff_algorithm = GX_ALGO_PARTITIONED;
+    double eff_load_factor = 0;
     // a batched run writes every sample's records into one buffer: the jobs share ownership
     std::shared_ptr<void> out_owner;
 };
@@ -131,6 +140,12 @@ gx_status guarded(const char *where, F &&f) {
         return GX_ECUDA;
     }
 }
+
+// The algorithm and fill a job runs with: its own options where set, else the context's
+// tuned choice for its key width, else the built-in defaults.
+void resolve_options(gx_job *j);
+// Fine-bucket fill aimed for by the partitioned build (distinct k-mers per 2048-slot table).
+double bucket_target(double load_factor);
 
 // Drops one reference to a context; the last one frees it.
 void ctx_release(gx_ctx *c);

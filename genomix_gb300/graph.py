@@ -106,6 +106,22 @@ class Context:
         _check(self._L.gx_ctx_elapsed_ms(self.h, a, b, ctypes.byref(ms)), "gx_ctx_elapsed_ms")
         return ms.value
 
+    def autotune(self, sample, k, repeats=2):
+        """gx_autotune: times every algorithm x fill on `sample` (readid text) and keeps the
+        fastest for jobs at the defaults; returns the choice and every candidate's time."""
+        r = _lib.TuneResult()
+        r.struct_size = ctypes.sizeof(_lib.TuneResult)
+        p, n, keep = _host_ptr(sample)
+        _check(self._L.gx_autotune(self.h, p, n, int(k), int(repeats), ctypes.byref(r)), "gx_autotune")
+        del keep
+        names = {_lib.ALGO_PARTITIONED: "partitioned", _lib.ALGO_TABLE: "table"}
+        return {"algorithm": names[r.algorithm], "load_factor": r.load_factor, "ms": r.ms,
+                "candidates": [{"algorithm": names[r.cand[i].algorithm], "load_factor": r.cand[i].load_factor,
+                                "ms": r.cand[i].ms} for i in range(r.tried)]}
+
+    def autotune_clear(self):
+        _check(self._L.gx_autotune_clear(self.h), "gx_autotune_clear")
+
     def synchronize(self):
         _check(self._L.gx_ctx_synchronize(self.h), "gx_ctx_synchronize")
 
@@ -131,7 +147,7 @@ class GraphBuildJob:
     """One graph build: inputs -> run() -> (VKmer, Node) records."""
 
     def __init__(self, ctx, kmer_length, input_kind="readid", paired=False, out_parts=1, load_factor=0.0,
-                 max_readids_per_edge=250, threads_per_read=0, est_input_bytes=0, algorithm="partitioned"):
+                 max_readids_per_edge=250, threads_per_read=0, est_input_bytes=0, algorithm="default"):
         self.ctx = ctx
         self._L = ctx._L
         kind = {"readid": _lib.INPUT_READID, "fastq": _lib.INPUT_FASTQ}[input_kind]

@@ -85,10 +85,11 @@ typedef struct gx_job_opts {
     int input_kind;           /* GX_INPUT_READID or GX_INPUT_FASTQ */
     int paired;               /* FASTQ only: 1 = mate streams 0 and 1 are paired files */
     int out_parts;            /* output parts (SequenceFile part files); 0 means 1 */
-    double load_factor;       /* fill of the hash tables aimed for; 0 = default (table build: slots =
-                                 occurrences / 0.5; partitioned build: 896 of 2048 per bucket) */
+    double load_factor;       /* fill of the hash tables aimed for; 0 = the context's autotuned choice,
+                                 else the built-in default (table build: slots = occurrences / 0.5;
+                                 partitioned build: 896 of 2048 per bucket) */
     int max_readids_per_edge; /* accepted and ignored, as in the reference (GenomixJobConf.java:718) */
-    int threads_per_read;     /* 0 = autotuned; 1 = thread per read; 32 = warp per read */
+    int threads_per_read;     /* reserved: every k-mer walk runs one thread per read */
     size_t est_input_bytes;   /* capacity hint for the device input buffer; 0 = grow on demand */
     int algorithm;            /* GX_ALGO_*: how occurrences are aggregated */
 } gx_job_opts;
@@ -121,6 +122,7 @@ typedef struct gx_stats {
     double ms_total;          /* device time of gx_job_run */
     double ms_aggregate;      /* device time of the per-bucket aggregation (part of ms_emit) */
     double ms_write;          /* device time of the record-writer kernel (part of ms_emit) */
+    uint64_t attempts;        /* passes run: 1, plus one per table/bucket overflow retried */
 } gx_stats;
 
 /* ---- context ------------------------------------------------------------------------- */
@@ -195,6 +197,32 @@ void gx_job_destroy(gx_job *job);
  * to statuses[i] (may be NULL); the call returns the first non-OK status.  Replaces running
  * one Hyracks job per read set (GenomixHyracksDriver.java:84-135 per sample). */
 gx_status gx_batch_run(gx_ctx *ctx, gx_job **jobs, int n, gx_status *statuses);
+
+/* ---- autotuning ------------------------------------------------------------------------ */
+
+#define GX_TUNE_MAX 16
+
+typedef struct gx_tune_result {
+    size_t struct_size;  /* sizeof(gx_tune_result), set by the caller */
+    int algorithm;       /* the fastest: GX_ALGO_PARTITIONED or GX_ALGO_TABLE */
+    double load_factor;  /* and its fill (partitioned: distinct k-mers per 2048-slot bucket table) */
+    double ms;           /* its device time on the sample */
+    int tried;
+    struct {
+        int algorithm;
+        double load_factor;
+        double ms;       /* best of the repeats; < 0 if the candidate failed */
+    } cand[GX_TUNE_MAX];
+} gx_tune_result;
+
+/* Time every candidate (algorithm x fill) on `sample` (readid text in host memory, e.g. the
+ * first tens of MB of a run's input) `repeats` times (0 = 2) and keep the fastest in the
+ * context for k-mers of k's key width (64-bit for k <= 32, 128-bit above): jobs created with
+ * GX_ALGO_DEFAULT and load_factor 0 then use it, in gx_job_run, gx_batch_run and serving.
+ * The reference has no counterpart (its sort-based aggregation has no such parameters). */
+gx_status gx_autotune(gx_ctx *ctx, const void *sample, size_t bytes, int k, int repeats, gx_tune_result *out);
+/* Forget the tuned choices: jobs at the defaults use the built-in settings again. */
+gx_status gx_autotune_clear(gx_ctx *ctx);
 
 /* ---- serving: graph builds admitted as they arrive ------------------------------------ */
 
