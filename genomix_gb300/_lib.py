@@ -18,6 +18,7 @@ STATUS_NAMES = {
 }
 INPUT_READID, INPUT_FASTQ = 0, 1
 ALGO_DEFAULT, ALGO_PARTITIONED, ALGO_TABLE = 0, 1, 2
+PLAN_BUILD_DEBRUIJN_GRAPH, PLAN_BUILD_READ_PARSER = 0, 1
 
 # every symbol include/gxgpu.h declares
 EXPORTS = [
@@ -27,7 +28,7 @@ EXPORTS = [
     "gx_pinned_free", "gx_fastq_to_readid", "gx_host_free", "gx_seqfile_write", "gx_seqfile_read",
     "gx_records_to_text", "gx_build_noalloc",
     "gx_serve_create", "gx_serve_submit", "gx_serve_poll", "gx_serve_stats_get", "gx_serve_destroy",
-    "gx_records_digest", "gx_autotune", "gx_autotune_clear",
+    "gx_records_digest", "gx_autotune", "gx_autotune_clear", "gx_job_graph_stats", "gx_seqfile_write_kmer_keys",
 ]
 
 
@@ -47,7 +48,8 @@ class JobOpts(ctypes.Structure):
         ("threads_per_read", ctypes.c_int),
         ("est_input_bytes", ctypes.c_size_t),
         ("algorithm", ctypes.c_int),
-    ]
+            ("plan", ctypes.c_int),
+]
 
 
 class ServeOpts(ctypes.Structure):
@@ -61,6 +63,40 @@ class ServeStats(ctypes.Structure):
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+STAT_BINS = 4096
+
+
+class StatHist(ctypes.Structure):
+    _fields_ = [("total", ctypes.c_uint64), ("maximum", ctypes.c_uint64), ("above", ctypes.c_uint64),
+                ("bins", ctypes.c_uint64 * STAT_BINS)]
+
+    def as_dict(self):
+        nz = {i: self.bins[i] for i in range(STAT_BINS) if self.bins[i]}
+        return {"total": self.total, "maximum": self.maximum, "above": self.above, "bins": nz}
+
+
+class GraphStats(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t),
+                ("nodes", ctypes.c_uint64), ("path_nodes", ctypes.c_uint64),
+                ("tips_reverse", ctypes.c_uint64), ("tips_forward", ctypes.c_uint64),
+                ("tips_both", ctypes.c_uint64), ("tips_one", ctypes.c_uint64),
+                ("self_edges", ctypes.c_uint64 * 4),
+                ("degree", StatHist), ("kmer_length", StatHist), ("coverage", StatHist),
+                ("unflipped_read_ids", StatHist), ("flipped_read_ids", StatHist), ("seed_score", StatHist),
+                ("kmer_length_with", StatHist * 2), ("coverage_with", StatHist * 2),
+                ("seed_score_with", StatHist * 2)]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f in ("nodes", "path_nodes", "tips_reverse", "tips_forward", "tips_both",
+                                           "tips_one")}
+        d["self_edges"] = list(self.self_edges)
+        for f in ("degree", "kmer_length", "coverage", "unflipped_read_ids", "flipped_read_ids", "seed_score"):
+            d[f] = getattr(self, f).as_dict()
+        for f in ("kmer_length_with", "coverage_with", "seed_score_with"):
+            d[f] = [getattr(self, f)[i].as_dict() for i in range(2)]
+        return d
 
 
 class TuneCand(ctypes.Structure):
@@ -141,6 +177,8 @@ def load():
         "gx_records_digest": ([vp, sz, P(Digest)], i),
         "gx_autotune": ([vp, vp, sz, i, i, P(TuneResult)], i),
         "gx_autotune_clear": ([vp], i),
+        "gx_job_graph_stats": ([vp, P(GraphStats)], i),
+        "gx_seqfile_write_kmer_keys": ([vp, sz, vp, ctypes.c_uint64, P(vp), P(sz)], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -92,7 +92,8 @@ static void write_text(std::string &o, const char *s) {
     o.append(s, n);
 }
 
-gx_status seqfile_write(const uint8_t *rec, size_t n, const uint8_t *sync_in, uint64_t seed, std::string &out) {
+gx_status seqfile_write(const uint8_t *rec, size_t n, const uint8_t *sync_in, uint64_t seed, std::string &out,
+                        const char *key_class) {
     uint8_t sync[16];
     if (sync_in) {
         memcpy(sync, sync_in, 16);
@@ -111,7 +112,7 @@ gx_status seqfile_write(const uint8_t *rec, size_t n, const uint8_t *sync_in, ui
     out.reserve(n + n / SYNC_INTERVAL * 20 + 256);
     // writeFileHeader: "SEQ" version 6, key/value class, compress flags, metadata, sync
     out.append("SEQ\x06", 4);
-    write_text(out, KEY_CLASS);
+    write_text(out, key_class ? key_class : KEY_CLASS);
     write_text(out, VAL_CLASS);
     out.push_back(0);  // compressed
     out.push_back(0);  // block compressed
@@ -527,7 +528,17 @@ gx_status gx_seqfile_write(const void *records, size_t bytes, const uint8_t *syn
                            size_t *out_bytes) {
     if ((!records && bytes) || !out || !out_bytes) return GX_EINVAL;
     std::string o;
-    gx_status st = gxh::seqfile_write((const uint8_t *)records, bytes, sync, seed, o);
+    gx_status st = gxh::seqfile_write((const uint8_t *)records, bytes, sync, seed, o, nullptr);
+    if (st != GX_OK) return st;
+    return give(o, (void **)out, out_bytes);
+}
+
+gx_status gx_seqfile_write_kmer_keys(const void *records, size_t bytes, const uint8_t *sync, uint64_t seed,
+                                     uint8_t **out, size_t *out_bytes) {
+    if ((!records && bytes) || !out || !out_bytes) return GX_EINVAL;
+    std::string o;
+    gx_status st = gxh::seqfile_write((const uint8_t *)records, bytes, sync, seed, o,
+                                      "edu.uci.ics.genomix.data.types.Kmer");
     if (st != GX_OK) return st;
     return give(o, (void **)out, out_bytes);
 }

@@ -9,6 +9,7 @@
 //   K5b  per-partition serialization
 // Device memory comes from the device's stream-ordered pool, kept warm between jobs.
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -156,11 +157,15 @@ static gx_status job_create_impl(gx_ctx *c, const gx_job_opts *opts, gx_job **ou
     if (opts->input_kind != GX_INPUT_READID && opts->input_kind != GX_INPUT_FASTQ) return GX_EINVAL;
     if (opts->out_parts < 0 || opts->load_factor < 0 || opts->load_factor > 0.95) return GX_EINVAL;
     if (opts->max_readids_per_edge < 0) return GX_EINVAL;  // GenomixJobConf.validateConf :456-457
+    const bool has_plan = opts->struct_size >= offsetof(gx_job_opts, plan) + sizeof(int);
+    if (has_plan && opts->plan != GX_PLAN_BUILD_DEBRUIJN_GRAPH && opts->plan != GX_PLAN_BUILD_READ_PARSER)
+        return GX_EINVAL;
     gx_job *j = new (std::nothrow) gx_job();
     if (!j) return GX_ENOMEM;
     j->ctx = c;
     c->refs.fetch_add(1);
-    j->o = *opts;
+    memcpy(&j->o, opts, std::min(sizeof j->o, opts->struct_size));
+    if (!has_plan) j->o.plan = GX_PLAN_BUILD_DEBRUIJN_GRAPH;
     if (j->o.out_parts == 0) j->o.out_parts = 1;
     j->k = opts->kmer_length;
     j->wide = j->k > 32 ? 1 : 0;
@@ -509,6 +514,62 @@ static gx_status build_table(RunCtx &rc) {
     }
 }
 
+// ---- the read-parser plan: every occurrence's (Kmer, Node) record, in read order -----------
+static gx_status build_read_parser(RunCtx &rc) {
+    gx_job *j = rc.j;
+    cudaStream_t s = rc.s;
+    Timers &tm = j->tm;
+    const uint32_t n = rc.n_reads;
+    RunArena tar(s);
+    unsigned long long *rbytes;
+    void *pscratch;
+    gx_status e;
+    if ((e = tar.alloc(rbytes, n)) != GX_OK) return e;
+    if ((e = tar.alloc(pscratch, scan_scratch_bytes((uint64_t)n + 1, 8))) != GX_OK) return e;
+    void *roff_v = nullptr, *outp = nullptr;
+    CK(cudaMallocAsync(&roff_v, (n + 1ull) * 8, s));
+    unsigned long long *roff = (unsigned long long *)roff_v;
+    CK(cudaEventRecord(tm.ev[2], s));
+    launch_rp_sizes(rc.lines, rc.reads, n, j->k, rbytes, s);
+    exclusive_scan_u64(rbytes, roff, n, roff + n, pscratch, s);
+    unsigned long long total = 0;
+    CK(cudaMemcpyAsync(&total, roff + n, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (cudaMallocAsync(&outp, total + 16, s) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFreeAsync(roff, s);
+        return GX_ENOMEM;
+    }
+    CK(cudaEventRecord(tm.ev[5], s));
+    launch_rp_write(j->wide, rc.text, rc.n_text, rc.lines, rc.reads, n, j->k, roff, (uint8_t *)outp, s);
+    CK(cudaEventRecord(tm.ev[6], s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    // output parts split between reads
+    const int P = j->o.out_parts;
+    for (int q = 0; q <= P; q++) {
+        unsigned long long v = total;
+        const uint64_t r = (uint64_t)n * q / P;
+        if (q < P && r > 0) CK(cudaMemcpy(&v, roff + r, 8, cudaMemcpyDeviceToHost));
+        if (q < P && r == 0) v = 0;
+        j->part_bounds[q] = v;
+    }
+    for (int q = 0; q < P; q++) j->cursor[q] = j->part_bounds[q];
+    j->d_out = (uint8_t *)outp;
+    j->out_bytes = total;
+    j->d_part_off = roff;  // record groups for chunked emits: one per read
+    j->nparts = n;
+    j->st.nodes = rc.n_occ;  // one record per occurrence
+    j->st.read_heads = n;
+    j->st.record_bytes = total;
+    j->st.table_partitions = n;
+    j->st.attempts = 1;
+    j->st.ms_write = tm.ms(5, 6);
+    j->st.ms_emit = tm.ms(2, 6);
+    j->st.ms_total = tm.ms(0, 6);
+    return GX_OK;
+}
+
 // ---- the partitioned build --------------------------------------------------------------
 static gx_status build_partitioned(RunCtx &rc) {
     gx_job *j = rc.j;
@@ -755,7 +816,7 @@ static gx_status run_job(gx_job *j) {
     j->st.key_bits = j->wide ? 128 : 64;
     const int k = j->k;
     resolve_options(j);
-    const bool partitioned = j->eff_algorithm != GX_ALGO_TABLE;
+    const bool partitioned = j->eff_algorithm != GX_ALGO_TABLE && j->o.plan == GX_PLAN_BUILD_DEBRUIJN_GRAPH;
     {
         const gx_status pe = prepare_text(j);
         if (pe != GX_OK) return pe;
@@ -842,6 +903,7 @@ static gx_status run_job(gx_job *j) {
     }
     rc.n_reads = n_reads;
     rc.n_occ = hs.n_occ;
+    if (j->o.plan == GX_PLAN_BUILD_READ_PARSER) return build_read_parser(rc);
     return partitioned ? build_partitioned(rc) : build_table(rc);
 }
 

@@ -2505,4 +2505,118 @@ void launch_emit_write_part(const EmitArgs &a, cudaStream_t s) {
     }
 }
 
+// ---- the BUILD_READ_PARSER plan ----------------------------------------------------------------
+//
+// JobGenReadLetterParser (genomix-hyracks/.../graph/job/JobGenReadLetterParser.java:60-147)
+// writes the parser's tuples unaggregated: one (Kmer, Node) SequenceFile record per k-mer
+// occurrence, in read order.  Per occurrence j of a read (ReadsKeyValueParserFactory.SplitReads,
+// :150-196, setEdgesForCurAndNext :209-233):
+//   key    the canonical k-mer, Kmer.write: its nb packed bytes (Kmer.java:344-346)
+//   value  a Node with coverage 1, one edge to the previous occurrence (type by the two
+//          orientations: FF->RR, FR->FR, RF->RF, RR->FF) and one to the next (FF, FR, RF, RR),
+//          and on the first occurrence the read head (unflipped at offset 0 or flipped at k-1).
+// Record sizes follow from the read lengths alone, so one scan places every record; one
+// thread per read walks its k-mers and writes them.
+// bytes of one read's records: n occurrences, n - 1 edges on each side, the head
+__device__ __forceinline__ unsigned long long rp_read_bytes(const LineRec &lr, uint32_t mate, int k) {
+    const uint32_t L = mate ? lr.l1 : lr.l0;
+    const unsigned long long n = L - (uint32_t)k + 1, nb = (uint32_t)(k + 3) / 4;
+    return n * (8 + nb + 1 + 4) + 2 * (n - 1) * (8 + nb) + 5 + head_bytes(lr, mate);
+}
+
+__global__ void k_rp_sizes(const LineRec *lines, const uint32_t *reads, uint32_t n_reads, int k,
+                           unsigned long long *rbytes) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_reads) return;
+    const uint32_t rl = reads[r];
+    rbytes[r] = rp_read_bytes(lines[rl >> 1], rl & 1u, k);
+}
+
+template <class K>
+__device__ __forceinline__ long long rp_key(const Sink &o, long long pos, K v, int nb) {
+    for (int i = 0; i < nb; i++) o.b(pos + i, KeyOps<K>::byte_at(v, nb - 1 - i));
+    return pos + nb;
+}
+
+template <class K>
+__global__ void k_rp_write(const uint8_t *text, unsigned long long n_text, const LineRec *lines,
+                           const uint32_t *reads, uint32_t n_reads, int k, const unsigned long long *roff,
+                           uint8_t *out) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_reads) return;
+    const Sink o{out, 0, 0, true};
+    const int nb = (k + 3) / 4;
+    const uint32_t rl = reads[r], mate = rl & 1u;
+    const LineRec lr = lines[rl >> 1];
+    Walker<K> w;
+    walker_for(w, text, n_text, lines, reads, r, k);
+    const uint32_t n = w.nk;
+    long long pos = (long long)roff[r];
+    K c, pc = 0, nc = 0;
+    uint32_t bits, d, pd = 0, nd = 0;
+    w.next(c, bits, d);
+    const uint32_t d0 = d;
+    for (uint32_t j = 0; j < n; j++) {
+        const bool has_next = j + 1 < n, has_prev = j > 0;
+        if (has_next) w.next(nc, bits, nd);
+        // edge types: from the previous occurrence, and to the next
+        const uint32_t tp = has_prev ? (pd == 0 ? (d == 0 ? 3u : 1u) : (d == 0 ? 2u : 0u)) : 4u;
+        const uint32_t tn = has_next ? 2u * d + nd : 4u;
+        uint32_t active = 0x80u;
+        if (has_prev) active |= 1u << tp;
+        if (has_next) active |= 1u << tn;
+        if (j == 0) active |= d0 == 0 ? 0x10u : 0x20u;
+        const long long st = pos;
+        pos += 8;
+        pos = rp_key<K>(o, pos, c, nb);
+        o.b(pos++, active);
+        for (uint32_t t = 0; t < 4; t++) {
+            if (t != tp && t != tn) continue;
+            o.u32(pos, 1);
+            o.u32(pos + 4, (uint32_t)k);
+            pos = rp_key<K>(o, pos + 8, t == tp ? pc : nc, nb);
+        }
+        if (j == 0) {
+            // the read head: ReadHeadSet with one ReadHeadInfo (ReadHeadInfo.write, :205-212)
+            const uint32_t L = mate ? lr.l1 : lr.l0, Lm = mate ? lr.l0 : lr.l1;
+            const unsigned long long uuid = ((unsigned long long)(d0 == 0 ? 0 : k - 1) << 40) |
+                                            ((unsigned long long)mate << 35) | (unsigned long long)lr.read_id;
+            o.b(pos, 1);
+            o.u32(pos + 1, 1);
+            o.b(pos + 5, Lm > 0 ? 1u : 0u);
+            o.u32(pos + 6, (uint32_t)(uuid >> 32));
+            o.u32(pos + 10, (uint32_t)uuid);
+            pos = put_seq(o, pos + 14, text + (mate ? lr.s1 : lr.s0), L);
+            if (Lm > 0) pos = put_seq(o, pos, text + (mate ? lr.s0 : lr.s1), Lm);
+        }
+        o.u32(pos, 0x3f800000u);  // coverage 1.0f
+        pos += 4;
+        o.u32(st, (uint32_t)(pos - st - 8));
+        o.u32(st + 4, (uint32_t)nb);
+        pc = c;
+        pd = d;
+        c = nc;
+        d = nd;
+    }
+}
+
+void launch_rp_sizes(const LineRec *lines, const uint32_t *reads, uint32_t n_reads, int k,
+                     unsigned long long *rbytes, cudaStream_t s) {
+    if (!n_reads) return;
+    t_launches++;
+    k_rp_sizes<<<(n_reads + 255) / 256, 256, 0, s>>>(lines, reads, n_reads, k, rbytes);
+}
+
+void launch_rp_write(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines, const uint32_t *reads,
+                     uint32_t n_reads, int k, const unsigned long long *roff, uint8_t *out, cudaStream_t s) {
+    if (!n_reads) return;
+    t_launches++;
+    if (wide)
+        k_rp_write<u128><<<(n_reads + 127) / 128, 128, 0, s>>>(text, n_text, lines, reads, n_reads, k, roff, out);
+    else
+        k_rp_write<uint64_t><<<(n_reads + 127) / 128, 128, 0, s>>>(text, n_text, lines, reads, n_reads, k, roff,
+                                                                    out);
+}
+
+
 }  // namespace gx

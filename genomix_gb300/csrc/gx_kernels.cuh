@@ -173,6 +173,12 @@ struct AggArgs {
     DevStatus *st;
 };
 void launch_aggregate(const AggArgs &a, cudaStream_t s);
+
+// the BUILD_READ_PARSER plan: bytes of each read's per-occurrence records, then the records
+void launch_rp_sizes(const LineRec *lines, const uint32_t *reads, uint32_t n_reads, int k,
+                     unsigned long long *rbytes, cudaStream_t s);
+void launch_rp_write(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines, const uint32_t *reads,
+                     uint32_t n_reads, int k, const unsigned long long *roff, uint8_t *out, cudaStream_t s);
 // record writer of the partitioned build (node offsets and head positions precomputed)
 void launch_emit_write_part(const EmitArgs &a, cudaStream_t s);
 

@@ -147,14 +147,17 @@ class GraphBuildJob:
     """One graph build: inputs -> run() -> (VKmer, Node) records."""
 
     def __init__(self, ctx, kmer_length, input_kind="readid", paired=False, out_parts=1, load_factor=0.0,
-                 max_readids_per_edge=250, threads_per_read=0, est_input_bytes=0, algorithm="default"):
+                 max_readids_per_edge=250, threads_per_read=0, est_input_bytes=0, algorithm="default",
+                 plan="BUILD_DEBRUIJN_GRAPH"):
         self.ctx = ctx
         self._L = ctx._L
         kind = {"readid": _lib.INPUT_READID, "fastq": _lib.INPUT_FASTQ}[input_kind]
         algo = {"default": _lib.ALGO_DEFAULT, "partitioned": _lib.ALGO_PARTITIONED, "table": _lib.ALGO_TABLE}[algorithm]
+        pl = {"BUILD_DEBRUIJN_GRAPH": _lib.PLAN_BUILD_DEBRUIJN_GRAPH, "BUILD_READ_PARSER": _lib.PLAN_BUILD_READ_PARSER}[plan]
         o = _lib.JobOpts(ctypes.sizeof(_lib.JobOpts), int(kmer_length), kind, 1 if paired else 0, int(out_parts),
                          float(load_factor), int(max_readids_per_edge), int(threads_per_read), int(est_input_bytes),
-                         algo)
+                         algo, pl)
+        self.plan = plan
         h = ctypes.c_void_p()
         _check(self._L.gx_job_create(ctx.h, ctypes.byref(o), ctypes.byref(h)), "gx_job_create")
         self.h = h.value
@@ -204,6 +207,14 @@ class GraphBuildJob:
         w, m = ctypes.c_size_t(), ctypes.c_int()
         _check(self._L.gx_job_emit(self.h, part, buf_ptr, cap, ctypes.byref(w), ctypes.byref(m)), "gx_job_emit")
         return w.value, bool(m.value)
+
+    def graph_stats(self):
+        """GraphStatistics counters of the job's graph, computed on the GPU (gx_job_graph_stats):
+        totals, maxima and value histograms (non-zero bins) of each statistic."""
+        g = _lib.GraphStats()
+        g.struct_size = ctypes.sizeof(_lib.GraphStats)
+        _check(self._L.gx_job_graph_stats(self.h, ctypes.byref(g)), "gx_job_graph_stats")
+        return g.as_dict()
 
     def rewind(self, part=None):
         """Restarts gx_job_emit at the beginning of one part (or of every part)."""
@@ -330,10 +341,12 @@ def fastq_to_readid(mate1: bytes, mate2: bytes = None) -> bytes:
     return data
 
 
-def seqfile_write(records: bytes, sync: bytes = None, seed: int = 0) -> bytes:
-    """A Hadoop SequenceFile<VKmer, Node> holding the record stream."""
+def seqfile_write(records: bytes, sync: bytes = None, seed: int = 0, key_class="VKmer") -> bytes:
+    """A Hadoop SequenceFile<VKmer, Node> (or <Kmer, Node>, the read-parser plan's files)
+    holding the record stream."""
     L = _lib.load()
-    st, data = _buf_out(L.gx_seqfile_write, records, len(records), sync, seed)
+    fn = {"VKmer": L.gx_seqfile_write, "Kmer": L.gx_seqfile_write_kmer_keys}[key_class]
+    st, data = _buf_out(fn, records, len(records), sync, seed)
     _check(st, "gx_seqfile_write")
     return data
 
@@ -389,9 +402,10 @@ def _input_files(paths):
 
 
 class GenomixGpuDriver:
-    """Drop-in for GenomixHyracksDriver for Plan.BUILD_DEBRUIJN_GRAPH."""
+    """Drop-in for GenomixHyracksDriver for Plan.BUILD_DEBRUIJN_GRAPH and Plan.BUILD_READ_PARSER."""
 
     BUILD_DEBRUIJN_GRAPH = "BUILD_DEBRUIJN_GRAPH"
+    BUILD_READ_PARSER = "BUILD_READ_PARSER"
 
     def __init__(self, device=0, threads_per_machine=1):
         self.ctx = Context(device)
@@ -400,8 +414,8 @@ class GenomixGpuDriver:
     def run_job(self, conf, plan=BUILD_DEBRUIJN_GRAPH, profile=False):
         """Reads the readid (or FASTQ) inputs named in conf, writes part-N SequenceFiles under
         the output directory, returns the job statistics."""
-        if plan != self.BUILD_DEBRUIJN_GRAPH:
-            raise ValueError(f"unsupported plan {plan}: only the graph build runs on the GPU")
+        if plan not in (self.BUILD_DEBRUIJN_GRAPH, self.BUILD_READ_PARSER):
+            raise ValueError(f"unsupported plan {plan}: the GPU runs the graph build and the read parser")
         k = int(conf[KMER_LENGTH])
         out_dir = conf[OUTPUT_DIR]
         parts = int(conf.get(THREADS_PER_MACHINE, self.threads_per_machine))
@@ -411,13 +425,13 @@ class GenomixGpuDriver:
         if fastq_pe or fastq_se:
             if fastq_pe:
                 fs = fastq_pe.split(",")
-                job = GraphBuildJob(self.ctx, k, "fastq", paired=True, out_parts=parts)
+                job = GraphBuildJob(self.ctx, k, "fastq", paired=True, out_parts=parts, plan=plan)
                 for a, b in zip(fs[0::2], fs[1::2]):
                     job.add_input(open(a, "rb").read(), 0)
                     job.add_input(open(b, "rb").read(), 1)
                 jobs.append(job)
             if fastq_se:
-                job = GraphBuildJob(self.ctx, k, "fastq", paired=False, out_parts=parts)
+                job = GraphBuildJob(self.ctx, k, "fastq", paired=False, out_parts=parts, plan=plan)
                 for a in fastq_se.split(","):
                     job.add_input(open(a, "rb").read(), 0)
                 jobs.append(job)
@@ -430,11 +444,11 @@ class GenomixGpuDriver:
                     text += fastq_to_readid(open(a, "rb").read())
                 for j in jobs:
                     j.close()
-                job = GraphBuildJob(self.ctx, k, "readid", out_parts=parts)
+                job = GraphBuildJob(self.ctx, k, "readid", out_parts=parts, plan=plan)
                 job.add_input(text)
                 jobs = [job]
         else:
-            job = GraphBuildJob(self.ctx, k, "readid", out_parts=parts)
+            job = GraphBuildJob(self.ctx, k, "readid", out_parts=parts, plan=plan)
             for f in _input_files(conf[INPUT_DIR].split(",")):
                 with open(f, "rb") as fh:
                     job.add_input(fh.read())
@@ -444,7 +458,8 @@ class GenomixGpuDriver:
         os.makedirs(out_dir, exist_ok=True)
         for q in range(job.out_parts):
             with open(os.path.join(out_dir, f"part-{q}"), "wb") as fh:
-                fh.write(seqfile_write(job.records(q), seed=q))
+                fh.write(seqfile_write(job.records(q), seed=q,
+                                       key_class="Kmer" if plan == self.BUILD_READ_PARSER else "VKmer"))
         st = job.stats()
         job.close()
         return st

@@ -92,7 +92,15 @@ typedef struct gx_job_opts {
     int threads_per_read;     /* reserved: every k-mer walk runs one thread per read */
     size_t est_input_bytes;   /* capacity hint for the device input buffer; 0 = grow on demand */
     int algorithm;            /* GX_ALGO_*: how occurrences are aggregated */
+    int plan;                 /* GX_PLAN_*: what the job writes */
 } gx_job_opts;
+
+/* Plans (gx_job_opts.plan), GenomixHyracksDriver.Plan (GenomixHyracksDriver.java:55-60). */
+enum {
+    GX_PLAN_BUILD_DEBRUIJN_GRAPH = 0,  /* one (VKmer, Node) record per distinct canonical k-mer */
+    GX_PLAN_BUILD_READ_PARSER = 1      /* one (Kmer, Node) record per k-mer occurrence, in read order,
+                                          unaggregated (JobGenReadLetterParser.java:60-147) */
+};
 
 /* Aggregation algorithms (gx_job_opts.algorithm); both give identical records. */
 enum {
@@ -197,6 +205,36 @@ void gx_job_destroy(gx_job *job);
  * to statuses[i] (may be NULL); the call returns the first non-OK status.  Replaces running
  * one Hyracks job per read set (GenomixHyracksDriver.java:84-135 per sample). */
 gx_status gx_batch_run(gx_ctx *ctx, gx_job **jobs, int n, gx_status *statuses);
+
+/* ---- graph statistics on the device-resident graph ------------------------------------- */
+
+#define GX_STAT_BINS 4096
+
+/* One statistic: its total over the nodes, its maximum, and how many nodes had each value
+ * (values >= GX_STAT_BINS are counted in `above`). */
+typedef struct gx_stat_hist {
+    uint64_t total, maximum, above;
+    uint64_t bins[GX_STAT_BINS];
+} gx_stat_hist;
+
+/* The counters GraphStatistics.map collects (genomix-hadoop/.../utils/GraphStatistics.java:
+ * 78-131) over a job's nodes: "totals", "maximum" and "<name>-bins" of each statistic. */
+typedef struct gx_graph_stats {
+    size_t struct_size;   /* sizeof(gx_graph_stats), set by the caller */
+    uint64_t nodes, path_nodes;
+    uint64_t tips_reverse, tips_forward, tips_both, tips_one;
+    uint64_t self_edges[4];                      /* selfEdge-FF, -FR, -RF, -RR */
+    gx_stat_hist degree, kmer_length, coverage;  /* coverage = Math.round(averageCoverage) */
+    gx_stat_hist unflipped_read_ids, flipped_read_ids;
+    gx_stat_hist seed_score;                     /* k * read heads, for coverage in 0 +- 1000 */
+    gx_stat_hist kmer_length_with[2], coverage_with[2], seed_score_with[2];  /* [0] REVERSE, [1] FORWARD */
+} gx_graph_stats;
+
+/* Statistics of a job's graph, computed on the GPU from its device-resident records (the
+ * graph never leaves the device).  Replaces the GraphStatistics MapReduce job run over the
+ * graph-build output (GraphStatistics.run, :136-152; GenomixDriver.java:120-137 for the
+ * coverage cutoff). */
+gx_status gx_job_graph_stats(gx_job *job, gx_graph_stats *out);
 
 /* ---- autotuning ------------------------------------------------------------------------ */
 
@@ -313,6 +351,11 @@ void gx_host_free(void *ptr);
  * opened in KmerNodePairSequenceWriterFactory.java:66-73.  *out is malloc'ed. */
 gx_status gx_seqfile_write(const void *records, size_t bytes, const uint8_t *sync, uint64_t seed,
                            uint8_t **out, size_t *out_bytes);
+
+/* The same container with key class edu.uci.ics.genomix.data.types.Kmer: the part files of
+ * the read-parser plan (JobGenReadLetterParser.java:100-103). */
+gx_status gx_seqfile_write_kmer_keys(const void *records, size_t bytes, const uint8_t *sync, uint64_t seed,
+                                     uint8_t **out, size_t *out_bytes);
 
 /* Extract the record stream from a SequenceFile written by gx_seqfile_write or by Hadoop
  * (uncompressed).  *out is malloc'ed. */

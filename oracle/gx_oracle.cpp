@@ -837,6 +837,31 @@ static Result build(const uint8_t *text, size_t n, int k, int threads, int parts
     return res;
 }
 
+// The BUILD_READ_PARSER plan (JobGenReadLetterParser.java:60-147): the parser's tuples as
+// they come, one (Kmer, Node) SequenceFile record per k-mer occurrence in read order.  The
+// key is Kmer.write: the nb packed bytes alone (Kmer.java:344-346).
+static int read_parser(const uint8_t *text, size_t n, int k, std::string &out, uint64_t &error_line,
+                       uint64_t &occurrences) {
+    std::vector<Line> lines;
+    split_lines(text, n, lines);
+    TupleStore ts;
+    Parser ps(k, ts);
+    for (size_t i = 0; i < lines.size(); i++) {
+        const int e = ps.parse(text + lines[i].begin, lines[i].end - lines[i].begin);
+        if (e != GX_OK) {
+            error_line = i + 1;
+            return e;
+        }
+    }
+    occurrences = ts.t.size();
+    for (size_t i = 0; i < ts.t.size(); i++) {
+        put_i32(out, (int32_t)(ts.t[i].klen + ts.t[i].vlen));
+        put_i32(out, (int32_t)ts.t[i].klen);
+        out.append((const char *)ts.key(i), ts.t[i].klen + ts.t[i].vlen);
+    }
+    return GX_OK;
+}
+
 // ---------------------------------------------------------------------------------------
 // Record streams: parse, normalise (the comparison form), text dump
 // ---------------------------------------------------------------------------------------
@@ -1070,6 +1095,19 @@ const uint64_t *gxo_result_part_offsets(const gxo_result *h, size_t *nparts) {
     return h->part_off.data();
 }
 void gxo_result_free(gxo_result *h) { delete h; }
+
+// Per-occurrence (Kmer, Node) records of the read-parser plan; *out is malloc'ed (gxo_free).
+int gxo_read_parser(const char *text, size_t n, int k, char **out, size_t *out_n, uint64_t *error_line,
+                    uint64_t *occurrences) {
+    std::string o;
+    *error_line = 0;
+    *occurrences = 0;
+    const int st = gxo::read_parser((const uint8_t *)text, n, k, o, *error_line, *occurrences);
+    *out = (char *)malloc(o.size() ? o.size() : 1);
+    memcpy(*out, o.data(), o.size());
+    *out_n = o.size();
+    return st;
+}
 
 static char *dup_out(const std::string &s, size_t *n) {
     char *p = (char *)malloc(s.size() + 1);

@@ -48,6 +48,10 @@ def lib():
                                           ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_size_t)]
         L.gxo_fastq_to_readid.restype = ctypes.c_int
         L.gxo_free.argtypes = [ctypes.c_void_p]
+        L.gxo_read_parser.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_size_t),
+                                      ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+        L.gxo_read_parser.restype = ctypes.c_int
         L.gxo_kat_kmer.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                    ctypes.c_char_p]
         L.gxo_kat_kmer_shift.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_char,
@@ -144,3 +148,14 @@ def java_float_to_string(f: float) -> str:
     out = ctypes.create_string_buffer(64)
     lib().gxo_kat_float_to_string(f, out)
     return out.value.decode()
+
+
+def read_parser(text: bytes, k: int):
+    """(status, error_line, occurrences, records) of the BUILD_READ_PARSER plan: one
+    (Kmer, Node) record per k-mer occurrence, in read order."""
+    L = lib()
+    p, n, el, occ = ctypes.c_void_p(), ctypes.c_size_t(), ctypes.c_uint64(), ctypes.c_uint64()
+    st = L.gxo_read_parser(text, len(text), k, ctypes.byref(p), ctypes.byref(n), ctypes.byref(el), ctypes.byref(occ))
+    rec = ctypes.string_at(p, n.value)
+    L.gxo_free(p)
+    return st, el.value, occ.value, rec
