@@ -13,6 +13,7 @@ from .graph import (
     Server,
     batch_run,
     fastq_to_readid,
+    fastq_to_readid_gpu,
     iter_records,
     records_digest,
     records_to_text,
@@ -22,5 +23,5 @@ from .graph import (
 
 __all__ = [
     "Context", "GenomixGpuDriver", "GraphBuildError", "GraphBuildJob", "PinnedBuffer", "Server", "batch_run",
-    "fastq_to_readid", "iter_records", "records_digest", "records_to_text", "seqfile_read", "seqfile_write",
+    "fastq_to_readid", "fastq_to_readid_gpu", "iter_records", "records_digest", "records_to_text", "seqfile_read", "seqfile_write",
 ]

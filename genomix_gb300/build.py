@@ -18,7 +18,7 @@ LIB = os.path.join(PKG, "libgxgpu.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SRCS = ["gx_kernels.cu", "gx_job.cu", "gx_batch.cu", "gx_serve.cu", "gx_tune.cu", "gx_graphstats.cu", "gx_noalloc.cu"]
+CUDA_SRCS = ["gx_kernels.cu", "gx_fastq.cu", "gx_job.cu", "gx_batch.cu", "gx_serve.cu", "gx_tune.cu", "gx_graphstats.cu", "gx_noalloc.cu"]
 CXX_SRCS = ["gx_formats.cpp"]
 
 

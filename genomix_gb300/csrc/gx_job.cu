@@ -12,6 +12,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <new>
 #include <string>
@@ -67,6 +68,42 @@ static gx_status append_text(gx_job *j, const void *src, size_t bytes, cudaMemcp
 }
 
 extern "C" {
+
+gx_status gx_fastq_to_readid_gpu(gx_ctx *c, const void *mate1, size_t bytes1, const void *mate2, size_t bytes2,
+                                 char **out, size_t *out_bytes) {
+    return guarded("gx_fastq_to_readid_gpu", [&]() -> gx_status {
+        if (!c || !out || !out_bytes || (!mate1 && bytes1)) return GX_EINVAL;
+        *out = nullptr;
+        *out_bytes = 0;
+        std::lock_guard<std::mutex> lk(c->mu);
+        cudaSetDevice(c->device);
+        cudaStream_t s = c->stream;
+        void *dev = nullptr;
+        uint64_t w = 0;
+        gx_status st = fastq_to_readid_device(
+            s, (const uint8_t *)mate1, bytes1, (const uint8_t *)mate2, bytes2,
+            [&](uint64_t total) -> uint8_t * {
+                if (cudaMallocAsync(&dev, total + 1, s) != cudaSuccess) {
+                    cudaGetLastError();
+                    dev = nullptr;
+                }
+                return (uint8_t *)dev;
+            },
+            w);
+        if (st == GX_OK) {
+            *out = (char *)malloc(w + 1);
+            if (!*out) {
+                st = GX_ENOMEM;
+            } else if (w) {
+                CK(cudaMemcpyAsync(*out, dev, w, cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+            }
+            *out_bytes = w;
+        }
+        if (dev) cudaFreeAsync(dev, s);
+        return st;
+    });
+}
 
 gx_status gx_pinned_alloc(size_t bytes, void **out) {
     if (!out) return GX_EINVAL;
@@ -784,22 +821,87 @@ static gx_status build_partitioned(RunCtx &rc) {
 
 namespace gxi {
 
+// line ends of one FASTQ file on the device; returns the line count
+static gx_status fastq_lines(cudaStream_t s, RunArena &ar, const uint8_t *d, uint64_t n, unsigned long long *&le,
+                             uint32_t &n_lines) {
+    const uint64_t tiles = line_tiles(n);
+    uint32_t *tile_cnt, *d_n;
+    void *scratch;
+    gx_status e;
+    if ((e = ar.alloc(tile_cnt, tiles + 1)) != GX_OK) return e;
+    if ((e = ar.alloc(d_n, 1)) != GX_OK) return e;
+    if ((e = ar.alloc(scratch, scan_scratch_bytes(std::max<uint64_t>(tiles, 1), 8))) != GX_OK) return e;
+    launch_count_lines(d, n, tile_cnt, s);
+    exclusive_scan_u32(tile_cnt, tile_cnt, tiles, d_n, scratch, s);
+    CK(cudaMemcpyAsync(&n_lines, d_n, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if ((e = ar.alloc(le, n_lines)) != GX_OK) return e;
+    launch_write_lines(d, n, tile_cnt, le, s);
+    return GX_OK;
+}
+
+gx_status fastq_to_readid_device(cudaStream_t s, const uint8_t *h1, size_t n1, const uint8_t *h2, size_t n2,
+                                 const std::function<uint8_t *(uint64_t)> &dest, uint64_t &written) {
+    written = 0;
+    RunArena ar(s);
+    uint8_t *d1, *d2 = nullptr;
+    gx_status e;
+    if ((e = ar.alloc(d1, n1 + 16)) != GX_OK) return e;
+    if (n1) CK(cudaMemcpyAsync(d1, h1, n1, cudaMemcpyHostToDevice, s));
+    if (h2) {
+        if ((e = ar.alloc(d2, n2 + 16)) != GX_OK) return e;
+        if (n2) CK(cudaMemcpyAsync(d2, h2, n2, cudaMemcpyHostToDevice, s));
+    }
+    unsigned long long *le1, *le2 = nullptr;
+    uint32_t nl1 = 0, nl2 = 0;
+    if ((e = fastq_lines(s, ar, d1, n1, le1, nl1)) != GX_OK) return e;
+    if (h2) {
+        if ((e = fastq_lines(s, ar, d2, n2, le2, nl2)) != GX_OK) return e;
+        if (nl1 != nl2) return GX_EFASTQ_PAIRING;  // GenomixDriver.java:682-686
+    }
+    const uint64_t n_rec = ((uint64_t)nl1 + 2) / 4;  // lines 1, 5, 9, ...
+    if (!n_rec) return GX_OK;
+    FqRec *rec;
+    unsigned long long *len, *off;
+    void *scratch;
+    if ((e = ar.alloc(rec, n_rec)) != GX_OK) return e;
+    if ((e = ar.alloc(len, n_rec)) != GX_OK) return e;
+    if ((e = ar.alloc(off, n_rec + 1)) != GX_OK) return e;
+    if ((e = ar.alloc(scratch, scan_scratch_bytes(n_rec + 1, 8))) != GX_OK) return e;
+    launch_fq_lines(d1, n1, le1, d2, n2, le2, n_rec, rec, len, s);
+    exclusive_scan_u64(len, off, n_rec, off + n_rec, scratch, s);
+    unsigned long long total = 0;
+    CK(cudaMemcpyAsync(&total, off + n_rec, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    uint8_t *out = dest(total);
+    if (!out) return GX_ENOMEM;
+    launch_fq_write(d1, d2, n_rec, rec, off, out, s);
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    written = total;
+    return GX_OK;
+}
+
 gx_status prepare_text(gx_job *j) {
-    cudaStream_t s = j->ctx->stream;
-    // FASTQ: the reference driver's conversion, then the readid path
+    // FASTQ: the reference driver's conversion (on the device), then the readid path
     if (j->o.input_kind == GX_INPUT_FASTQ) {
         const size_t nf = j->fastq[0].size();
         if (j->o.paired && j->fastq[1].size() != nf) return GX_EFASTQ_PAIRING;
         for (size_t f = 0; f < nf; f++) {
-            std::string txt;
             const std::string &a = j->fastq[0][f];
             const std::string *b = j->o.paired ? &j->fastq[1][f] : nullptr;
-            gx_status st = gxh::fastq_to_readid((const uint8_t *)a.data(), a.size(),
-                                                b ? (const uint8_t *)b->data() : nullptr, b ? b->size() : 0, txt);
-            if (st != GX_OK) return st;
-            st = append_text(j, txt.data(), txt.size(), cudaMemcpyHostToDevice, true);
-            if (st != GX_OK) return st;
-            CK(cudaStreamSynchronize(s));
+            gx_status grow = GX_OK;
+            uint64_t w = 0;
+            const gx_status st = fastq_to_readid_device(
+                j->ctx->stream, (const uint8_t *)a.data(), a.size(), b ? (const uint8_t *)b->data() : nullptr,
+                b ? b->size() : 0,
+                [&](uint64_t total) -> uint8_t * {
+                    grow = ensure_text_cap(j, j->text_len + total);
+                    return grow == GX_OK ? j->d_text + j->text_len : nullptr;
+                },
+                w);
+            if (st != GX_OK) return grow != GX_OK ? grow : st;
+            j->text_len += w;
         }
         j->fastq[0].clear();
         j->fastq[1].clear();

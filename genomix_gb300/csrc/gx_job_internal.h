@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cstdio>
 #include <exception>
+#include <functional>
 #include <memory>
 #include <new>
 #include <mutex>
@@ -154,5 +155,9 @@ void ctx_release(gx_ctx *c);
 gx_status run_job_locked(gx_job *j);
 // FASTQ inputs converted to readid text on the device (the reference driver's pre-pass).
 gx_status prepare_text(gx_job *j);
+// One FASTQ file (pair) to readid text on the device: `dest(total)` gives the device buffer
+// for the total bytes (null: out of memory).
+gx_status fastq_to_readid_device(cudaStream_t s, const uint8_t *h1, size_t n1, const uint8_t *h2, size_t n2,
+                                 const std::function<uint8_t *(uint64_t)> &dest, uint64_t &written);
 
 }  // namespace gxi

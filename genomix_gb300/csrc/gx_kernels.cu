@@ -15,7 +15,7 @@
 
 namespace gx {
 
-static thread_local uint64_t t_launches = 0;
+thread_local uint64_t t_launches = 0;  // kernels this host thread launched
 uint64_t launches_this_thread() { return t_launches; }
 
 // =========================================================================================

@@ -22,6 +22,7 @@ constexpr uint32_t EMIT_STAGE_BYTES = 16384;  // output staging window per parti
 
 // Kernel launches made by the calling host thread (read before and after a run).
 uint64_t launches_this_thread();
+extern thread_local uint64_t t_launches;  // incremented by every launcher
 
 // ---- scans (device-wide, exclusive) -----------------------------------------------------
 // Scratch needed by exclusive_scan for n items of T.
@@ -173,6 +174,17 @@ struct AggArgs {
     DevStatus *st;
 };
 void launch_aggregate(const AggArgs &a, cudaStream_t s);
+
+// FASTQ -> readid on the device: each record's trimmed sequence line(s) and output length,
+// then the readid lines at their scanned offsets
+struct FqRec {
+    unsigned long long b1, e1, b2, e2;
+};
+void launch_fq_lines(const uint8_t *t1, uint64_t n1, const unsigned long long *le1, const uint8_t *t2, uint64_t n2,
+                     const unsigned long long *le2, uint64_t n_rec, FqRec *rec, unsigned long long *len,
+                     cudaStream_t s);
+void launch_fq_write(const uint8_t *t1, const uint8_t *t2, uint64_t n_rec, const FqRec *rec,
+                     const unsigned long long *off, uint8_t *out, cudaStream_t s);
 
 // the BUILD_READ_PARSER plan: bytes of each read's per-occurrence records, then the records
 void launch_rp_sizes(const LineRec *lines, const uint32_t *reads, uint32_t n_reads, int k,

@@ -341,6 +341,20 @@ def fastq_to_readid(mate1: bytes, mate2: bytes = None) -> bytes:
     return data
 
 
+def fastq_to_readid_gpu(ctx, mate1: bytes, mate2: bytes = None) -> bytes:
+    """The same conversion on the GPU (gx_fastq_to_readid_gpu), as jobs with FASTQ input run it."""
+    L = ctx._L
+    out, n = ctypes.c_void_p(), ctypes.c_size_t()
+    p1, n1, k1 = _host_ptr(mate1)
+    p2, n2, k2 = _host_ptr(mate2) if mate2 is not None else (None, 0, None)
+    _check(L.gx_fastq_to_readid_gpu(ctx.h, p1, n1, p2, n2, ctypes.byref(out), ctypes.byref(n)),
+           "gx_fastq_to_readid_gpu")
+    data = ctypes.string_at(out, n.value) if n.value else b""
+    L.gx_host_free(out)
+    del k1, k2
+    return data
+
+
 def seqfile_write(records: bytes, sync: bytes = None, seed: int = 0, key_class="VKmer") -> bytes:
     """A Hadoop SequenceFile<VKmer, Node> (or <Kmer, Node>, the read-parser plan's files)
     holding the record stream."""

@@ -342,6 +342,10 @@ void gx_pinned_free(void *ptr);
  * *out is allocated with malloc; free it with gx_host_free. */
 gx_status gx_fastq_to_readid(const void *mate1, size_t bytes1, const void *mate2, size_t bytes2,
                              char **out, size_t *out_bytes);
+/* The same conversion run on the GPU of `ctx` (what jobs with GX_INPUT_FASTQ do): byte for
+ * byte gx_fastq_to_readid's output.  *out is malloc'ed (gx_host_free). */
+gx_status gx_fastq_to_readid_gpu(gx_ctx *ctx, const void *mate1, size_t bytes1, const void *mate2, size_t bytes2,
+                                 char **out, size_t *out_bytes);
 void gx_host_free(void *ptr);
 
 /* Write one Hadoop SequenceFile (version 6, uncompressed, key class
