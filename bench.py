@@ -428,12 +428,14 @@ def run_gb300(args, ws, rank, local):
     ctx = gx.Context(local)
     torch.cuda.set_device(local)
     # the autotuner picks algorithm and fill on a prefix of the workload (untimed)
-    tune = None if args.no_autotune else ctx.autotune(sample_prefix(w.text, TUNE_PAIRS), w.k)
+    tune = None if (args.no_autotune or args.fill) else ctx.autotune(sample_prefix(w.text, TUNE_PAIRS), w.k)
     d_text = torch.frombuffer(bytearray(w.text), dtype=torch.uint8).to(f"cuda:{local}")
     torch.cuda.synchronize()
 
+    pin = {"algorithm": "partitioned", "load_factor": args.fill} if args.fill else {}
+
     def step_device():
-        job = gx.GraphBuildJob(ctx, w.k)
+        job = gx.GraphBuildJob(ctx, w.k, **pin)
         job.add_input_device(d_text.data_ptr(), d_text.numel())
         job.run()
         st = job.stats()
@@ -464,7 +466,7 @@ def run_gb300(args, ws, rank, local):
     pin_out = gx.PinnedBuffer(out_bytes + 16)
 
     def step_e2e():
-        job = gx.GraphBuildJob(ctx, w.k)
+        job = gx.GraphBuildJob(ctx, w.k, **pin)
         job.add_input(pin_in)
         job.run()
         wr, more = job.emit_into(0, pin_out.ptr, pin_out.nbytes)
@@ -552,6 +554,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the served-stream measurement")
     ap.add_argument("--no-autotune", action="store_true", help="run with the built-in settings")
     ap.add_argument("--no-long-k", action="store_true", help="skip the 50 Mbp k = 55 measurement")
+    ap.add_argument("--fill", type=float, default=0.0,
+                    help="partitioned build at this bucket fill instead of the autotuner's choice (profiling runs)")
     ap.add_argument("--max-pairs", type=int, default=None,
                     help="use only the first pairs of the workload (profiling captures)")
     args = ap.parse_args()

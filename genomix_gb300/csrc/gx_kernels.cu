@@ -1866,17 +1866,30 @@ struct AggSmem {
     K key1[AGG_SLOTS];
     uint32_t cnt[AGG_SLOTS];
     uint32_t meta[AGG_SLOTS];
-    uint32_t nbytes[AGG_SLOTS];   // record bytes per node, then its offset
+    uint32_t nbytes[AGG_SLOTS];   // keys per home while ordering; then record bytes per node, then offsets
     uint16_t ord[AGG_SLOTS];
     uint16_t rank_of_slot[AGG_SLOTS];
-    uint32_t cu[AGG_SLOTS], cf[AGG_SLOTS];  // unflipped / flipped heads per node
-    uint32_t hstart[AGG_SLOTS];   // first kept head of each node
+    uint16_t home[AGG_SLOTS];     // home slot of each occupied slot's key
     unsigned long long ws[33];
     unsigned long long carry;
     uint32_t n, fail, kept;
 };
 
 constexpr int AGG_BATCH = 8;  // occurrence loads in flight per thread
+
+// first of the kept head keys (sorted) that is >= x
+__device__ __forceinline__ uint32_t kept_lower_bound(const unsigned long long *hk, uint32_t kept,
+                                                     unsigned long long x) {
+    uint32_t lo = 0, hi = kept;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (hk[mid] < x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
 
 template <class K>
 __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
@@ -1889,16 +1902,13 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
     const uint16_t *obits = a.obits2 + o0;
     const uint32_t M = (uint32_t)(o1 - o0);
     {
-        const uint4 z = make_uint4(0, 0, 0, 0), ones = make_uint4(~0u, ~0u, ~0u, ~0u);
+        const uint4 z = make_uint4(0, 0, 0, 0);
         uint4 *k4 = reinterpret_cast<uint4 *>(sm.key1);
         for (uint32_t i = threadIdx.x; i < AGG_SLOTS * sizeof(K) / 16; i += blockDim.x) k4[i] = z;
         for (uint32_t i = threadIdx.x; i < AGG_SLOTS / 4; i += blockDim.x) {
             reinterpret_cast<uint4 *>(sm.cnt)[i] = z;
             reinterpret_cast<uint4 *>(sm.meta)[i] = z;
             reinterpret_cast<uint4 *>(sm.nbytes)[i] = z;
-            reinterpret_cast<uint4 *>(sm.cu)[i] = z;
-            reinterpret_cast<uint4 *>(sm.cf)[i] = z;
-            reinterpret_cast<uint4 *>(sm.hstart)[i] = ones;
         }
     }
     if (threadIdx.x == 0) {
@@ -1922,12 +1932,16 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
             const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
             if (i >= M) continue;
             uint32_t claimed = 0;
-            const int sl = AggTable<K>::insert(sm.key1, kk[q], (uint32_t)KeyOps<K>::hash(kk[q]), claimed);
+            const uint32_t h = (uint32_t)KeyOps<K>::hash(kk[q]);
+            const int sl = AggTable<K>::insert(sm.key1, kk[q], h, claimed);
             if (sl < 0) {
                 sm.fail = 1;
                 continue;
             }
-            if (claimed) atomicAdd(&sm.n, 1u);
+            if (claimed) {
+                atomicAdd(&sm.n, 1u);
+                sm.home[sl] = (uint16_t)(h & (AGG_SLOTS - 1));  // where its probe started
+            }
             atomicAdd(&sm.cnt[sl], 1u);
             if (bb[q]) atomicOr(&sm.meta[sl], bb[q]);
         }
@@ -1954,34 +1968,30 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
     }
     __syncthreads();
     // 3. order the nodes deterministically: by home slot (the low hash bits that started the
-    //    probe), then by key: a counting sort over the 2048 home slots; a home holds one or
-    //    two keys at this load, ordered by the thread that owns the home
-    for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x) {
-        const K k1 = sm.key1[i];
-        if (k1 != (K)0) atomicAdd(&sm.cu[(uint32_t)KeyOps<K>::hash(k1 - 1) & (AGG_SLOTS - 1)], 1u);
-    }
+    //    probe), then by key.  A counting sort over the 2048 homes: keys per home (nbytes),
+    //    their offsets, then each key's place among the keys of its home, counted back along
+    //    its probe run (the keys of one home all lie between the home and the key's slot)
+    for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x)
+        if (sm.key1[i] != (K)0) atomicAdd(&sm.nbytes[sm.home[i]], 1u);
     __syncthreads();
-    block_scan_array(sm.cu, AGG_SLOTS, reinterpret_cast<uint32_t *>(sm.ws));
+    const uint32_t n_keys = block_scan_array(sm.nbytes, AGG_SLOTS, reinterpret_cast<uint32_t *>(sm.ws));
     for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x) {
-        const K k1 = sm.key1[i];
-        if (k1 == (K)0) continue;
-        const uint32_t hm = (uint32_t)KeyOps<K>::hash(k1 - 1) & (AGG_SLOTS - 1);
-        sm.ord[sm.cu[hm] + atomicAdd(&sm.cf[hm], 1u)] = (uint16_t)i;
+        if (sm.key1[i] == (K)0) continue;
+        const uint32_t hm = sm.home[i];
+        uint32_t before = 0;
+        for (uint32_t j = hm; j != i; j = (j + 1) & (AGG_SLOTS - 1))
+            if (sm.key1[j] != (K)0 && sm.home[j] == hm) before++;
+        sm.ord[sm.nbytes[hm] + before] = (uint16_t)i;
     }
     __syncthreads();
     for (uint32_t hm = threadIdx.x; hm < AGG_SLOTS; hm += blockDim.x) {
-        const uint32_t b0 = sm.cu[hm], c = sm.cf[hm];
+        const uint32_t b0 = sm.nbytes[hm], c = (hm + 1 < AGG_SLOTS ? sm.nbytes[hm + 1] : n_keys) - b0;
         for (uint32_t u = 1; u < c; u++)
             for (uint32_t v = b0 + u; v > b0 && sm.key1[sm.ord[v]] < sm.key1[sm.ord[v - 1]]; v--) {
                 const uint16_t t = sm.ord[v];
                 sm.ord[v] = sm.ord[v - 1];
                 sm.ord[v - 1] = t;
             }
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x) {
-        sm.cu[i] = 0;
-        sm.cf[i] = 0;
     }
     const uint32_t n = sm.n;
     __syncthreads();
@@ -2058,11 +2068,6 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
             const uint32_t rank = (uint32_t)(key >> 37);
             const uint32_t rl = a.reads[r];
             atomicAdd(&sm.nbytes[rank], head_bytes(a.lines[rl >> 1], rl & 1u));
-            if ((key >> 36) & 1ULL)
-                atomicAdd(&sm.cf[rank], 1u);
-            else
-                atomicAdd(&sm.cu[rank], 1u);
-            atomicMin(&sm.hstart[rank], w);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -2117,11 +2122,15 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
         const unsigned long long key = hk[i];
         const uint32_t rank = (uint32_t)(key >> 37);
         const bool flipped = (key >> 36) & 1ULL;
-        const uint32_t st = sm.hstart[rank];
+        // the node's kept heads: [st, st + cu) unflipped, then cf flipped (hk is sorted by
+        // rank, flipped, position)
+        const unsigned long long rbase = (unsigned long long)rank << 37;
+        const uint32_t st = kept_lower_bound(hk, kept, rbase);
+        const uint32_t fl = kept_lower_bound(hk, kept, rbase | (1ULL << 36));
+        const uint32_t cu = fl - st, cf = kept_lower_bound(hk, kept, rbase + (1ULL << 37)) - fl;
         const unsigned long long pre = key & ((1ULL << 36) - 1);
         const unsigned long long pre0 = hk[st] & ((1ULL << 36) - 1);
         const uint32_t meta = sm.meta[sm.ord[rank]];
-        const uint32_t cu = sm.cu[rank], cf = sm.cf[rank];
         uint32_t edges = 0;
         for (int t = 0; t < 4; t++) {
             const uint32_t m = (meta >> (4 * t)) & 15u;
