@@ -29,7 +29,7 @@ EXPORTS = [
     "gx_records_to_text", "gx_build_noalloc",
     "gx_serve_create", "gx_serve_submit", "gx_serve_poll", "gx_serve_stats_get", "gx_serve_destroy",
     "gx_records_digest", "gx_autotune", "gx_autotune_clear", "gx_job_graph_stats", "gx_seqfile_write_kmer_keys",
-    "gx_fastq_to_readid_gpu",
+    "gx_fastq_to_readid_gpu", "gx_job_emit_async", "gx_job_emit_wait",
 ]
 
 
@@ -181,6 +181,8 @@ def load():
         "gx_job_graph_stats": ([vp, P(GraphStats)], i),
         "gx_seqfile_write_kmer_keys": ([vp, sz, vp, ctypes.c_uint64, P(vp), P(sz)], i),
         "gx_fastq_to_readid_gpu": ([vp, vp, sz, vp, sz, P(vp), P(sz)], i),
+        "gx_job_emit_async": ([vp, i, vp, sz, P(sz), P(i)], i),
+        "gx_job_emit_wait": ([vp], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -105,10 +105,10 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
     bool any_borrowed = false;
     for (uint32_t i = 0; i < n; i++)
         if (jobs[i]->text_borrowed && jobs[i]->text_len) {
-            CK(cudaMemcpyAsync(&lastb[i], jobs[i]->d_text + jobs[i]->text_len - 1, 1, cudaMemcpyDeviceToHost, s));
+            CK(d2h_async(&lastb[i], jobs[i]->d_text + jobs[i]->text_len - 1, 1, s));
             any_borrowed = true;
         }
-    if (any_borrowed) CK(cudaStreamSynchronize(s));
+    if (any_borrowed) CK(sync_stream(s));
     std::vector<unsigned long long> tb(n + 1, 0);
     for (uint32_t i = 0; i < n; i++) tb[i + 1] = tb[i] + jobs[i]->text_len + (lastb[i] != '\n' ? 1 : 0);
     const uint64_t n_text = tb[n];
@@ -158,8 +158,8 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
     launch_count_lines(text, n_text, tile_cnt, s);
     exclusive_scan_u32(tile_cnt, tile_cnt, tiles, d_nlines, scratch, s);
     uint32_t n_lines = 0;
-    CK(cudaMemcpyAsync(&n_lines, d_nlines, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    CK(d2h_async(&n_lines, d_nlines, 4, s));
+    CK(sync_stream(s));
     unsigned long long *line_end;
     LineRec *lines;
     uint8_t *lflags;
@@ -178,12 +178,12 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
     CK(cudaEventRecord(tm.ev[1], s));
     DevStatus hs;
     std::vector<uint32_t> h_lb(n + 1), h_rb(n + 1), h_scnt((size_t)n * MAX_SUPERS), h_hll((size_t)n * HLL_REGS);
-    CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(h_lb.data(), line_base, (n + 1) * 4ull, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(h_rb.data(), read_base, (n + 1) * 4ull, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(h_scnt.data(), d_scnt, h_scnt.size() * 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(h_hll.data(), d_hll, h_hll.size() * 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    CK(d2h_async(&hs, d_st, sizeof hs, s));
+    CK(d2h_async(h_lb.data(), line_base, (n + 1) * 4ull, s));
+    CK(d2h_async(h_rb.data(), read_base, (n + 1) * 4ull, s));
+    CK(d2h_async(h_scnt.data(), d_scnt, h_scnt.size() * 4, s));
+    CK(d2h_async(h_hll.data(), d_hll, h_hll.size() * 4, s));
+    CK(sync_stream(s));
     CK(cudaGetLastError());
     if (hs.parse_err != ~0ULL) return BATCH_FALLBACK;  // every job reruns alone for its own status
 
@@ -320,9 +320,9 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         exclusive_scan_u64(part_bytes, part_off, P, part_off + P, pscratch, s);
         CK(cudaEventRecord(tm.ev[4], s));
         unsigned long long total = 0;
-        CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(&total, part_off + P, 8, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
+        CK(d2h_async(&hs, d_st, sizeof hs, s));
+        CK(d2h_async(&total, part_off + P, 8, s));
+        CK(sync_stream(s));
         CK(cudaGetLastError());
         if (hs.internal_err) {
             fprintf(stderr, "gxgpu: internal error: a read head's k-mer was not aggregated\n");
@@ -370,11 +370,11 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         CK(cudaEventRecord(tm.ev[6], s));
         std::vector<unsigned long long> h_po(P + 1);
         std::vector<uint32_t> h_pn(P), h_hc(P);
-        CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(h_po.data(), part_off, (P + 1) * 8ull, cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(h_pn.data(), part_nodes, P * 4ull, cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(h_hc.data(), head_cnt2, P * 4ull, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
+        CK(d2h_async(&hs, d_st, sizeof hs, s));
+        CK(d2h_async(h_po.data(), part_off, (P + 1) * 8ull, s));
+        CK(d2h_async(h_pn.data(), part_nodes, P * 4ull, s));
+        CK(d2h_async(h_hc.data(), head_cnt2, P * 4ull, s));
+        CK(sync_stream(s));
         CK(cudaGetLastError());
         if (hs.internal_err) {
             fprintf(stderr, "gxgpu: internal error: record sizes disagree between emission passes\n");

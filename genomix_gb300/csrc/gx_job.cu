@@ -96,7 +96,7 @@ gx_status gx_fastq_to_readid_gpu(gx_ctx *c, const void *mate1, size_t bytes1, co
                 st = GX_ENOMEM;
             } else if (w) {
                 CK(cudaMemcpyAsync(*out, dev, w, cudaMemcpyDeviceToHost, s));
-                CK(cudaStreamSynchronize(s));
+                CK(sync_stream(s));
             }
             *out_bytes = w;
         }
@@ -146,6 +146,11 @@ gx_status gx_ctx_create(int device, const gx_ctx_opts *opts, gx_ctx **out) {
     cudaMemGetInfo(&fr, &tot);
     c->mem_limit = (opts && opts->device_mem_limit) ? opts->device_mem_limit : (size_t)(0.9 * (double)fr);
     for (auto &e : c->marks) cudaEventCreate(&e);
+    if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return GX_ECUDA;
+    }
     *out = c;
     return GX_OK;
 }
@@ -153,7 +158,7 @@ gx_status gx_ctx_create(int device, const gx_ctx_opts *opts, gx_ctx **out) {
 void gx_ctx_destroy(gx_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
+    sync_stream(c->stream);
     ctx_release(c);
 }
 
@@ -177,7 +182,7 @@ gx_status gx_ctx_elapsed_ms(gx_ctx *c, int a, int b, double *ms) {
 gx_status gx_ctx_synchronize(gx_ctx *c) {
     if (!c) return GX_EINVAL;
     cudaSetDevice(c->device);
-    CK(cudaStreamSynchronize(c->stream));
+    CK(sync_stream(c->stream));
     return GX_OK;
 }
 
@@ -232,7 +237,7 @@ static gx_status job_add_input_impl(gx_job *j, const void *host, size_t bytes, i
     const bool nl = bytes > 0 && ((const uint8_t *)host)[bytes - 1] == '\n';
     gx_status st = append_text(j, host, bytes, cudaMemcpyHostToDevice, nl);
     if (st != GX_OK) return st;
-    CK(cudaStreamSynchronize(j->ctx->stream));  // the host buffer is only borrowed for this call
+    CK(sync_stream(j->ctx->stream));  // the host buffer is only borrowed for this call
     return GX_OK;
 }
 
@@ -255,12 +260,13 @@ gx_status gx_job_add_input_device(gx_job *j, const void *dev, size_t bytes, int 
         return GX_OK;
     }
     uint8_t last = 0;
-    CK(cudaMemcpyAsync(&last, (const uint8_t *)dev + bytes - 1, 1, cudaMemcpyDeviceToHost, j->ctx->stream));
-    CK(cudaStreamSynchronize(j->ctx->stream));
+    CK(d2h_async(&last, (const uint8_t *)dev + bytes - 1, 1, j->ctx->stream));
+    CK(sync_stream(j->ctx->stream));
     if (j->text_borrowed && j->text_len) {
         // make the borrowed first input end with a terminator before appending
         uint8_t l0 = 0;
-        CK(cudaMemcpy(&l0, j->d_text + j->text_len - 1, 1, cudaMemcpyDeviceToHost));
+        CK(d2h_async(&l0, j->d_text + j->text_len - 1, 1, j->ctx->stream));
+        CK(sync_stream(j->ctx->stream));
         gx_status st = ensure_text_cap(j, j->text_len + bytes + 2);
         if (st != GX_OK) return st;
         if (l0 != '\n') {
@@ -295,18 +301,41 @@ gx_status gx_job_records_device(gx_job *j, const void **dev, size_t *bytes, cons
     return GX_OK;
 }
 
-static gx_status job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *written, int *more);
+static gx_status job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *written, int *more,
+                          bool async);
 
 gx_status gx_job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *written, int *more) {
-    return guarded("gx_job_emit", [&] { return job_emit(j, part, host_out, cap, written, more); });
+    return guarded("gx_job_emit", [&] { return job_emit(j, part, host_out, cap, written, more, false); });
 }
 
-static gx_status job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *written, int *more) {
+gx_status gx_job_emit_async(gx_job *j, int part, void *host_out, size_t cap, size_t *written, int *more) {
+    return guarded("gx_job_emit_async", [&] { return job_emit(j, part, host_out, cap, written, more, true); });
+}
+
+static gx_status wait_copy(gx_job *j) {
+    if (!j->copy_pending) return GX_OK;
+    j->copy_pending = false;
+    CK(cudaEventSynchronize(j->ev_copy));
+    return GX_OK;
+}
+
+gx_status gx_job_emit_wait(gx_job *j) {
+    if (!j) return GX_EINVAL;
+    cudaSetDevice(j->ctx->device);
+    return wait_copy(j);
+}
+
+static gx_status job_emit(gx_job *j, int part, void *host_out, size_t cap, size_t *written, int *more,
+                          bool async) {
     if (!j || !written || !more || (!host_out && cap)) return GX_EINVAL;
     if (j->state != JS_RAN) return GX_ESTATE;
     if (part < 0 || part >= j->o.out_parts) return GX_EINVAL;
     std::lock_guard<std::mutex> lk(j->ctx->mu);
     cudaSetDevice(j->ctx->device);
+    if (!async) {
+        gx_status we = wait_copy(j);
+        if (we != GX_OK) return we;
+    }
     const uint64_t end = j->part_bounds[part + 1];
     uint64_t cur = j->cursor[part];
     *written = 0;
@@ -343,8 +372,22 @@ static gx_status job_emit(gx_job *j, int part, void *host_out, size_t cap, size_
             return GX_OK;
         }
     }
-    CK(cudaMemcpyAsync(host_out, j->d_out + cur, stop - cur, cudaMemcpyDeviceToHost, j->ctx->stream));
-    CK(cudaStreamSynchronize(j->ctx->stream));
+    if (async) {
+        // the build is complete (runs end synchronized): the copy needs no other dependency.  It
+        // runs on the copy stream, alongside whatever the context's stream does next, in pieces:
+        // copies in one direction share a copy engine, and the small status reads of a build
+        // running meanwhile then wait for one piece, not for the whole copy
+        if (!j->ev_copy) CK(cudaEventCreateWithFlags(&j->ev_copy, cudaEventDisableTiming));
+        const uint64_t piece = 32ull << 20;
+        for (uint64_t o = cur; o < stop; o += piece)
+            CK(cudaMemcpyAsync((uint8_t *)host_out + (o - cur), j->d_out + o, std::min<uint64_t>(piece, stop - o),
+                               cudaMemcpyDeviceToHost, j->ctx->copy_stream));
+        CK(cudaEventRecord(j->ev_copy, j->ctx->copy_stream));
+        j->copy_pending = true;
+    } else {
+        CK(cudaMemcpyAsync(host_out, j->d_out + cur, stop - cur, cudaMemcpyDeviceToHost, j->ctx->stream));
+        CK(sync_stream(j->ctx->stream));
+    }
     j->cursor[part] = stop;
     *written = stop - cur;
     *more = stop < end ? 1 : 0;
@@ -353,6 +396,8 @@ static gx_status job_emit(gx_job *j, int part, void *host_out, size_t cap, size_
 
 gx_status gx_job_emit_rewind(gx_job *j, int part) {
     if (!j) return GX_EINVAL;
+    cudaSetDevice(j->ctx->device);
+    if (wait_copy(j) != GX_OK) return GX_ECUDA;
     if (j->state != JS_RAN) return GX_ESTATE;
     if (part < -1 || part >= j->o.out_parts) return GX_EINVAL;
     for (int q = 0; q < j->o.out_parts; q++)
@@ -365,6 +410,8 @@ void gx_job_destroy(gx_job *j) {
     {
         std::lock_guard<std::mutex> lk(j->ctx->mu);
         cudaSetDevice(j->ctx->device);
+        wait_copy(j);  // an asynchronous emit still reading the records
+        if (j->ev_copy) cudaEventDestroy(j->ev_copy);
         cudaStream_t s = j->ctx->stream;
         if (j->d_text && !j->text_borrowed) cudaFreeAsync(j->d_text, s);
         if (j->out_owner)
@@ -372,7 +419,7 @@ void gx_job_destroy(gx_job *j) {
         else if (j->d_out)
             cudaFreeAsync(j->d_out, s);
         if (j->d_part_off) cudaFreeAsync(j->d_part_off, s);
-        cudaStreamSynchronize(s);
+        sync_stream(s);
         j->tm.destroy();
     }
     gx_ctx *c = j->ctx;
@@ -413,13 +460,15 @@ static gx_status finish_outputs(RunCtx &rc, uint32_t nparts, unsigned long long 
         if (q == P)
             v = total;
         else if (tp > 0)
-            CK(cudaMemcpy(&v, part_off + tp, 8, cudaMemcpyDeviceToHost));
+            CK(d2h_async(&v, part_off + tp, 8, rc.s));
+        CK(sync_stream(rc.s));
         j->part_bounds[q] = v;
     }
     for (int q = 0; q < P; q++) j->cursor[q] = j->part_bounds[q];
     std::vector<uint32_t> pn(nparts), hc(nparts);
-    CK(cudaMemcpy(pn.data(), part_nodes, nparts * 4ull, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(hc.data(), head_cnt2, nparts * 4ull, cudaMemcpyDeviceToHost));
+    CK(d2h_async(pn.data(), part_nodes, nparts * 4ull, rc.s));
+    CK(d2h_async(hc.data(), head_cnt2, nparts * 4ull, rc.s));
+    CK(sync_stream(rc.s));
     uint64_t nn = 0, nh = 0;
     for (uint32_t q = 0; q < nparts; q++) {
         nn += pn[q];
@@ -503,9 +552,9 @@ static gx_status build_table(RunCtx &rc) {
         exclusive_scan_u64(part_bytes, part_off, nparts, part_off + nparts, pscratch, s);
         CK(cudaEventRecord(tm.ev[4], s));
         unsigned long long total = 0;
-        CK(cudaMemcpyAsync(&hs, rc.d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(&total, part_off + nparts, 8, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
+        CK(d2h_async(&hs, rc.d_st, sizeof hs, s));
+        CK(d2h_async(&total, part_off + nparts, 8, s));
+        CK(sync_stream(s));
         CK(cudaGetLastError());
         if (hs.table_full) {
             cudaFreeAsync(part_off, s);
@@ -527,8 +576,8 @@ static gx_status build_table(RunCtx &rc) {
         CK(cudaEventRecord(tm.ev[5], s));
         launch_emit_write(a, s);
         CK(cudaEventRecord(tm.ev[6], s));
-        CK(cudaMemcpyAsync(&hs, rc.d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
+        CK(d2h_async(&hs, rc.d_st, sizeof hs, s));
+        CK(sync_stream(s));
         CK(cudaGetLastError());
         if (hs.internal_err) {
             cudaFreeAsync(outp, s);
@@ -570,8 +619,8 @@ static gx_status build_read_parser(RunCtx &rc) {
     launch_rp_sizes(rc.lines, rc.reads, n, j->k, rbytes, s);
     exclusive_scan_u64(rbytes, roff, n, roff + n, pscratch, s);
     unsigned long long total = 0;
-    CK(cudaMemcpyAsync(&total, roff + n, 8, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    CK(d2h_async(&total, roff + n, 8, s));
+    CK(sync_stream(s));
     if (cudaMallocAsync(&outp, total + 16, s) != cudaSuccess) {
         cudaGetLastError();
         cudaFreeAsync(roff, s);
@@ -580,14 +629,17 @@ static gx_status build_read_parser(RunCtx &rc) {
     CK(cudaEventRecord(tm.ev[5], s));
     launch_rp_write(j->wide, rc.text, rc.n_text, rc.lines, rc.reads, n, j->k, roff, (uint8_t *)outp, s);
     CK(cudaEventRecord(tm.ev[6], s));
-    CK(cudaStreamSynchronize(s));
+    CK(sync_stream(s));
     CK(cudaGetLastError());
     // output parts split between reads
     const int P = j->o.out_parts;
     for (int q = 0; q <= P; q++) {
         unsigned long long v = total;
         const uint64_t r = (uint64_t)n * q / P;
-        if (q < P && r > 0) CK(cudaMemcpy(&v, roff + r, 8, cudaMemcpyDeviceToHost));
+        if (q < P && r > 0) {
+            CK(d2h_async(&v, roff + r, 8, s));
+            CK(sync_stream(s));
+        }
         if (q < P && r == 0) v = 0;
         j->part_bounds[q] = v;
     }
@@ -743,9 +795,9 @@ static gx_status build_partitioned(RunCtx &rc) {
         exclusive_scan_u64(part_bytes, part_off, P, part_off + P, pscratch, s);
         CK(cudaEventRecord(tm.ev[4], s));
         unsigned long long total = 0;
-        CK(cudaMemcpyAsync(&hs, rc.d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(&total, part_off + P, 8, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
+        CK(d2h_async(&hs, rc.d_st, sizeof hs, s));
+        CK(d2h_async(&total, part_off + P, 8, s));
+        CK(sync_stream(s));
         CK(cudaGetLastError());
         if (hs.internal_err) {
             cudaFreeAsync(part_off, s);
@@ -795,8 +847,8 @@ static gx_status build_partitioned(RunCtx &rc) {
         CK(cudaEventRecord(tm.ev[5], s));
         launch_emit_write_part(a, s);
         CK(cudaEventRecord(tm.ev[6], s));
-        CK(cudaMemcpyAsync(&hs, rc.d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
+        CK(d2h_async(&hs, rc.d_st, sizeof hs, s));
+        CK(sync_stream(s));
         CK(cudaGetLastError());
         if (hs.internal_err) {
             cudaFreeAsync(outp, s);
@@ -833,8 +885,8 @@ static gx_status fastq_lines(cudaStream_t s, RunArena &ar, const uint8_t *d, uin
     if ((e = ar.alloc(scratch, scan_scratch_bytes(std::max<uint64_t>(tiles, 1), 8))) != GX_OK) return e;
     launch_count_lines(d, n, tile_cnt, s);
     exclusive_scan_u32(tile_cnt, tile_cnt, tiles, d_n, scratch, s);
-    CK(cudaMemcpyAsync(&n_lines, d_n, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    CK(d2h_async(&n_lines, d_n, 4, s));
+    CK(sync_stream(s));
     if ((e = ar.alloc(le, n_lines)) != GX_OK) return e;
     launch_write_lines(d, n, tile_cnt, le, s);
     return GX_OK;
@@ -871,12 +923,12 @@ gx_status fastq_to_readid_device(cudaStream_t s, const uint8_t *h1, size_t n1, c
     launch_fq_lines(d1, n1, le1, d2, n2, le2, n_rec, rec, len, s);
     exclusive_scan_u64(len, off, n_rec, off + n_rec, scratch, s);
     unsigned long long total = 0;
-    CK(cudaMemcpyAsync(&total, off + n_rec, 8, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    CK(d2h_async(&total, off + n_rec, 8, s));
+    CK(sync_stream(s));
     uint8_t *out = dest(total);
     if (!out) return GX_ENOMEM;
     launch_fq_write(d1, d2, n_rec, rec, off, out, s);
-    CK(cudaStreamSynchronize(s));
+    CK(sync_stream(s));
     CK(cudaGetLastError());
     written = total;
     return GX_OK;
@@ -959,8 +1011,8 @@ static gx_status run_job(gx_job *j) {
     launch_count_lines(text, n_text, tile_cnt, s);
     exclusive_scan_u32(tile_cnt, tile_cnt, tiles, d_nlines, scratch, s);
     uint32_t n_lines = 0;
-    CK(cudaMemcpyAsync(&n_lines, d_nlines, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    CK(d2h_async(&n_lines, d_nlines, 4, s));
+    CK(sync_stream(s));
     j->st.lines = n_lines;
     unsigned long long *line_end;
     LineRec *lines;
@@ -982,15 +1034,15 @@ static gx_status run_job(gx_job *j) {
     DevStatus hs;
     uint32_t n_reads = 0;
     RunCtx rc{j, s, ar, d_st, scratch, text, n_text, lines, reads, n_lines, 0, 0, d_scnt, d_hll, {}, {}};
-    CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(&n_reads, d_nlines + 1, 4, cudaMemcpyDeviceToHost, s));
+    CK(d2h_async(&hs, d_st, sizeof hs, s));
+    CK(d2h_async(&n_reads, d_nlines + 1, 4, s));
     if (partitioned) {
         rc.scnt.resize(MAX_SUPERS);
         rc.hll.resize(HLL_REGS);
-        CK(cudaMemcpyAsync(rc.scnt.data(), d_scnt, MAX_SUPERS * 4, cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(rc.hll.data(), d_hll, HLL_REGS * 4, cudaMemcpyDeviceToHost, s));
+        CK(d2h_async(rc.scnt.data(), d_scnt, MAX_SUPERS * 4, s));
+        CK(d2h_async(rc.hll.data(), d_hll, HLL_REGS * 4, s));
     }
-    CK(cudaStreamSynchronize(s));
+    CK(sync_stream(s));
     CK(cudaGetLastError());
     if (hs.parse_err != ~0ULL) {
         j->st.error_line = (hs.parse_err >> 8) + 1;
@@ -1026,7 +1078,9 @@ double gxi::bucket_target(double load_factor) {
 void gxi::ctx_release(gx_ctx *c) {
     if (c->refs.fetch_sub(1) != 1) return;
     cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
+    sync_stream(c->stream);
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
     for (auto &e : c->marks)
         if (e) cudaEventDestroy(e);
     cudaStreamDestroy(c->stream);

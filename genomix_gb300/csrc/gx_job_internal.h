@@ -43,6 +43,7 @@ struct Timers {
 struct gx_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // gx_job_emit_async copies: they overlap the next build
     std::mutex mu;
     size_t mem_limit = 0;
     cudaEvent_t marks[16] = {};
@@ -80,6 +81,8 @@ struct gx_job {
     std::vector<unsigned long long> h_part_off;  // lazily fetched copy of d_part_off
     gx_stats st{};
     gxi::Timers tm;
+    cudaEvent_t ev_copy = nullptr;  // the last asynchronous emit's copy
+    bool copy_pending = false;
     // the algorithm and fill this run uses: the job's options, or the context's tuned choice
     int eff_algorithm = GX_ALGO_PARTITIONED;
     double eff_load_factor = 0;

@@ -8,6 +8,8 @@
 //   K5  compaction + serialization     outputFinalResult (:185-214), Node.write,
 //                                      KmerNodePairSequenceWriterFactory.write (:79-94)
 #include <algorithm>
+#include <cstring>
+#include <vector>
 #include <cmath>
 #include <cstdio>
 
@@ -17,6 +19,74 @@ namespace gx {
 
 thread_local uint64_t t_launches = 0;  // kernels this host thread launched
 uint64_t launches_this_thread() { return t_launches; }
+
+// ---- device -> host reads through mapped pinned memory -----------------------------------------
+__global__ void k_readback(const uint8_t *__restrict__ src, uint8_t *__restrict__ dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+namespace {
+struct Stage {
+    uint8_t *p = nullptr;  // pinned, mapped (unified addressing: the same pointer on the device)
+    size_t cap = 0, used = 0;
+    cudaStream_t s = nullptr;
+    struct Pending {
+        void *dst;
+        size_t off, n;
+    };
+    std::vector<Pending> pend;
+};
+thread_local Stage t_stage;
+
+cudaError_t deliver(Stage &b) {
+    for (const Stage::Pending &q : b.pend) memcpy(q.dst, b.p + q.off, q.n);
+    b.pend.clear();
+    b.used = 0;
+    return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t sync_stream(cudaStream_t s) {
+    const cudaError_t e = cudaStreamSynchronize(s);
+    Stage &b = t_stage;
+    if (e == cudaSuccess && !b.pend.empty() && b.s == s) deliver(b);
+    return e;
+}
+
+cudaError_t d2h_async(void *dst, const void *src, size_t n, cudaStream_t s) {
+    if (!n) return cudaSuccess;
+    Stage &b = t_stage;
+    if (!b.pend.empty() && b.s != s) {  // reads of another stream first
+        const cudaError_t e = cudaStreamSynchronize(b.s);
+        if (e != cudaSuccess) return e;
+        deliver(b);
+    }
+    const size_t sz = (n + 15) & ~(size_t)15;
+    if (b.used + sz > b.cap) {
+        if (!b.pend.empty()) {
+            const cudaError_t e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return e;
+            deliver(b);
+        }
+        if (sz > b.cap) {
+            if (b.p) cudaFreeHost(b.p);
+            b.p = nullptr;
+            b.cap = 0;
+            const size_t cap = std::max<size_t>(sz, 16u << 20);
+            const cudaError_t e = cudaMallocHost((void **)&b.p, cap);
+            if (e != cudaSuccess) return e;
+            b.cap = cap;
+        }
+    }
+    const unsigned blocks = (unsigned)std::min<size_t>((n + 4095) / 4096, 64);
+    t_launches++;
+    k_readback<<<blocks, 256, 0, s>>>((const uint8_t *)src, b.p + b.used, n);
+    b.pend.push_back(Stage::Pending{dst, b.used, n});
+    b.used += sz;
+    b.s = s;
+    return cudaGetLastError();
+}
 
 // =========================================================================================
 // scans

@@ -22,6 +22,14 @@ constexpr uint32_t EMIT_STAGE_BYTES = 16384;  // output staging window per parti
 
 // Kernel launches made by the calling host thread (read before and after a run).
 uint64_t launches_this_thread();
+
+// Device -> host reads of a build (counts, status, offsets).  A small kernel copies the bytes
+// into this thread's mapped pinned staging buffer, so no copy engine is involved: a large
+// record copy running on a copy engine meanwhile (gx_job_emit_async) cannot delay them.
+// d2h_async queues one read on stream s; sync_stream synchronizes s and delivers the queued
+// reads to their host destinations.
+cudaError_t d2h_async(void *dst, const void *src, size_t bytes, cudaStream_t s);
+cudaError_t sync_stream(cudaStream_t s);
 extern thread_local uint64_t t_launches;  // incremented by every launcher
 
 // ---- scans (device-wide, exclusive) -----------------------------------------------------

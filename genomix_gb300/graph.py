@@ -220,6 +220,17 @@ class GraphBuildJob:
         """Restarts gx_job_emit at the beginning of one part (or of every part)."""
         _check(self._L.gx_job_emit_rewind(self.h, -1 if part is None else part), "gx_job_emit_rewind")
 
+    def emit_async(self, part, buf_ptr, cap):
+        """gx_job_emit_async: queues the copy of (the next piece of) a part; (written, more).
+        The buffer is ready after emit_wait()."""
+        w, m = ctypes.c_size_t(), ctypes.c_int()
+        _check(self._L.gx_job_emit_async(self.h, part, buf_ptr, cap, ctypes.byref(w), ctypes.byref(m)),
+               "gx_job_emit_async")
+        return w.value, bool(m.value)
+
+    def emit_wait(self):
+        _check(self._L.gx_job_emit_wait(self.h), "gx_job_emit_wait")
+
     def records(self, part=None, chunk=None):
         """Serialized record stream of one part (or all parts in order) as bytes."""
         parts = range(self.out_parts) if part is None else [part]

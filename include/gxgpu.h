@@ -179,6 +179,14 @@ gx_status gx_job_run(gx_job *job);
  * stopped; *more is 1 while bytes remain.  Each call ends on a record boundary. */
 gx_status gx_job_emit(gx_job *job, int part, void *host_out, size_t cap, size_t *written, int *more);
 
+/* gx_job_emit, but the copy is only queued (on the context's copy stream, which runs beside its
+ * build stream): it overlaps whatever the context does next, e.g. the next job's build.  The
+ * host buffer must not be read or reused until gx_job_emit_wait(job) returns; any other call
+ * on the job waits for the copy first.  *written and *more are final when the call returns.
+ * No counterpart in the reference (its writer streams to HDFS synchronously). */
+gx_status gx_job_emit_async(gx_job *job, int part, void *host_out, size_t cap, size_t *written, int *more);
+gx_status gx_job_emit_wait(gx_job *job);
+
 /* Restart gx_job_emit of output part `part` (-1: every part) from its first record. */
 gx_status gx_job_emit_rewind(gx_job *job, int part);
 

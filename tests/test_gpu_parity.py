@@ -255,3 +255,29 @@ def test_job_outlives_its_context():
     rec = job.records()
     job.close()
     assert go.normalize(rec) == go.normalize(go.build_graph(text, 21).records)
+
+
+def test_async_emit_pipeline(ctx):
+    texts = [synth.small_random(80 + i, 1500, 120, 31, paired=True) for i in range(4)]
+    want = [gpu_build(ctx, t, 31)[0] for t in texts]
+    bufs = [gx.PinnedBuffer(max(len(r) for r in want) + 16) for _ in range(2)]
+    prev = None
+    got = [None] * 4
+    for i, t in enumerate(texts):
+        job = gx.GraphBuildJob(ctx, 31)
+        job.add_input(t)
+        job.run()
+        w, more = job.emit_async(0, bufs[i % 2].ptr, bufs[i % 2].nbytes)
+        assert not more and w == len(want[i])
+        if prev is not None:
+            pj, pi, pw = prev
+            pj.emit_wait()
+            got[pi] = bytes(bufs[pi % 2].array()[:pw])
+            pj.close()
+        prev = (job, i, w)
+    pj, pi, pw = prev
+    pj.close()  # destroy waits for the copy
+    got[pi] = bytes(bufs[pi % 2].array()[:pw])
+    assert got == want
+    for b in bufs:
+        b.close()
