@@ -1616,6 +1616,13 @@ struct SuperSmem {
     static size_t bytes(uint32_t S) { return sizeof(SuperSmem) + 3ull * S * sizeof(uint32_t); }
 };
 
+// 64-bit keys keep a round's k-mers in registers between counting and placing them; 128-bit
+// keys walk the round twice instead (their cache would cost too many registers)
+template <class K> struct SuperRound {
+    static constexpr bool CACHE = sizeof(K) == 8;
+    static constexpr int N = CACHE ? 10 : SC_ROUND;  // k-mers per thread per round
+};
+
 template <class K>
 __global__ void __launch_bounds__(SC_THREADS) k_scatter_super(const uint8_t *text, unsigned long long n_text,
                                                               const LineRec *lines,
@@ -1623,6 +1630,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_scatter_super(const uint8_t *tex
                                                               SampleMap m, uint32_t S,
                                                               const unsigned long long *s_off,
                                                               uint32_t *s_cur, K *okey, uint16_t *obits) {
+    constexpr bool CACHE = SuperRound<K>::CACHE;
+    constexpr int RN = SuperRound<K>::N;
     extern __shared__ __align__(16) uint8_t smem_raw[];
     SuperSmem<K> &sm = *reinterpret_cast<SuperSmem<K> *>(smem_raw);
     uint32_t *const sm_loff = sm.arrays, *const sm_gbase = sm.arrays + S, *const sm_cur = sm.arrays + 2 * S;
@@ -1639,19 +1648,29 @@ __global__ void __launch_bounds__(SC_THREADS) k_scatter_super(const uint8_t *tex
     }
     if (threadIdx.x == 0) sm.rounds = 0;
     __syncthreads();
-    atomicMax(&sm.rounds, (w.nk + SC_ROUND - 1) / SC_ROUND);
+    atomicMax(&sm.rounds, (w.nk + RN - 1) / RN);
     __syncthreads();
     const uint32_t rounds = sm.rounds;
+    K ck[CACHE ? RN : 1];
+    uint32_t cb[CACHE ? RN : 1];  // edge bits | super << 16
     for (uint32_t round = 0; round < rounds; round++) {
         for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) sm_cur[i] = 0;
         __syncthreads();
         const Walker<K> w0 = w;
+        const uint32_t nq = w.j < w.nk ? min((uint32_t)RN, w.nk - w.j) : 0u;
         // count this round's occurrences per super bucket
-        for (int q = 0; q < SC_ROUND && !w.done(); q++) {
+#pragma unroll
+        for (int q = 0; q < RN; q++) {
+            if ((uint32_t)q >= nq) break;
             K c;
             uint32_t b, d;
             w.next(c, b, d);
-            atomicAdd(&sm_cur[sbase + super_local(KeyOps<K>::hash(c), log_s)], 1u);
+            const uint32_t sp = sbase + super_local(KeyOps<K>::hash(c), log_s);
+            atomicAdd(&sm_cur[sp], 1u);
+            if (CACHE) {
+                ck[q] = c;
+                cb[q] = b | (sp << 16);
+            }
         }
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) {
@@ -1663,12 +1682,21 @@ __global__ void __launch_bounds__(SC_THREADS) k_scatter_super(const uint8_t *tex
         for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) sm_cur[i] = 0;
         __syncthreads();
         // place them in shared memory grouped by super bucket
-        w = w0;
-        for (int q = 0; q < SC_ROUND && !w.done(); q++) {
+        if (!CACHE) w = w0;
+#pragma unroll
+        for (int q = 0; q < RN; q++) {
+            if ((uint32_t)q >= nq) break;
             K c;
-            uint32_t b, d;
-            w.next(c, b, d);
-            const uint32_t sp = sbase + super_local(KeyOps<K>::hash(c), log_s);
+            uint32_t b, sp;
+            if (CACHE) {
+                c = ck[q];
+                b = cb[q] & 0xffffu;
+                sp = cb[q] >> 16;
+            } else {
+                uint32_t d;
+                w.next(c, b, d);
+                sp = sbase + super_local(KeyOps<K>::hash(c), log_s);
+            }
             const uint32_t pos = sm_loff[sp] + atomicAdd(&sm_cur[sp], 1u);
             sm.key[pos] = c;
             sm.bits[pos] = (uint16_t)b;
