@@ -1969,6 +1969,8 @@ struct AggSmem {
     uint16_t rank_of_slot[AGG_SLOTS];
     uint16_t home[AGG_SLOTS];     // home slot of each occupied slot's key
     unsigned long long ws[33];
+    unsigned long long wsk[32];   // warp 0's head sort
+    uint32_t wsv[32];
     unsigned long long carry;
     uint32_t n, fail, kept;
 };
@@ -2103,76 +2105,118 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
         nkey[j] = sm.key1[o] - 1;
         ncm[j] = (unsigned long long)sm.cnt[o] | ((unsigned long long)sm.meta[o] << 32);
         if (sm.cnt[o] >= (1u << 24)) inexact++;
+        sm.nbytes[j] = node_base_bytes(sm.meta[o], nb);
     }
     if (inexact) atomicAdd(&a.st->cov_inexact, inexact);
     __syncthreads();
-    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) sm.nbytes[j] = node_base_bytes(sm.meta[sm.ord[j]], nb);
-    // 5. read heads: sort by (node, TreeSet order), keep the first of equal uuids
-    // (the sort runs in global scratch: a bucket holds few heads)
+    // 5. read heads: sort by (node, TreeSet order), keep the first of equal uuids.  A bucket
+    //    with at most 32 heads (the usual case) leaves them to warp 0, in registers; larger
+    //    ones sort in global scratch with the whole block.
     unsigned long long *hk = a.head_sk + hb;
     uint32_t *hv = a.head_idx + hb;
-    if (hc > HEAD_CAP && threadIdx.x == 0) atomicAdd(&a.st->big_head_parts, 1u);
-    for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
-        const uint32_t r = hv[i];
-        const Head h = a.heads[r];
-        hk[i] = head_sort_key(sm.rank_of_slot[h.slot], h.uuid);
-    }
-    __syncthreads();
-    if (hc <= blockDim.x) {
-        // few heads (the usual case): each thread places its own by counting the smaller
-        // (key, read) pairs; read ordinals are distinct, so the ranks are too
-        unsigned long long mk = 0;
-        uint32_t mv = 0, rank = 0;
-        if (threadIdx.x < hc) {
-            mk = hk[threadIdx.x];
-            mv = hv[threadIdx.x];
-            for (uint32_t j = 0; j < hc; j++) {
-                const unsigned long long kj = hk[j];
-                const uint32_t vj = hv[j];
+    const int lane = threadIdx.x & 31;
+    const bool warp_heads = hc <= 32;
+    unsigned long long wk = 0;  // warp path: this lane's head in sorted order, kept or not
+    uint32_t wv = 0, wkeep = 0, wkept_idx = 0, wkeep_mask = 0;
+    if (warp_heads) {
+        if (threadIdx.x < 32) {
+            unsigned long long mk = ~0ULL;
+            uint32_t mv = 0xffffffffu;
+            if (lane < (int)hc) {
+                mv = hv[lane];
+                const Head h = a.heads[mv];
+                mk = head_sort_key(sm.rank_of_slot[h.slot], h.uuid);
+            }
+            uint32_t rank = 0;
+            for (int j = 0; j < (int)hc; j++) {
+                const unsigned long long kj = __shfl_sync(0xffffffffu, mk, j);
+                const uint32_t vj = __shfl_sync(0xffffffffu, mv, j);
                 rank += (kj < mk || (kj == mk && vj < mv)) ? 1u : 0u;
             }
-        }
-        __syncthreads();
-        if (threadIdx.x < hc) {
-            hk[rank] = mk;
-            hv[rank] = mv;
+            if (lane < (int)hc) {
+                sm.wsk[rank] = mk;
+                sm.wsv[rank] = mv;
+            }
+            __syncwarp();
+            if (lane < (int)hc) {
+                wk = sm.wsk[lane];
+                wv = sm.wsv[lane];
+            }
+            const unsigned long long prev = __shfl_up_sync(0xffffffffu, wk, 1);
+            wkeep = (lane < (int)hc && (lane == 0 || wk != prev)) ? 1u : 0u;
+            wkeep_mask = __ballot_sync(0xffffffffu, wkeep);
+            wkept_idx = __popc(wkeep_mask & ((1u << lane) - 1u));
+            if (wkeep) {
+                const uint32_t rl = a.reads[wv];
+                atomicAdd(&sm.nbytes[(uint32_t)(wk >> 37)], head_bytes(a.lines[rl >> 1], rl & 1u));
+            }
+            if (lane == 0) sm.kept = __popc(wkeep_mask);
         }
         __syncthreads();
     } else {
-        bitonic_sort_pairs<unsigned long long, uint32_t>(hk, hv, hc);
-    }
-    if (threadIdx.x == 0) {
-        sm.kept = 0;
-        sm.carry = 0;
-    }
-    __syncthreads();
-    for (uint32_t c0 = 0; c0 < hc; c0 += blockDim.x) {
-        const uint32_t i = c0 + threadIdx.x;
-        unsigned long long key = 0;
-        uint32_t keep = 0, r = 0;
-        if (i < hc) {
-            key = hk[i];
-            const unsigned long long prev = i == 0 ? ~0ULL : (i == c0 ? sm.carry : hk[i - 1]);
-            keep = key != prev ? 1u : 0u;
-            r = hv[i];
-        }
-        const unsigned long long last = hk[min(hc, c0 + blockDim.x) - 1];
-        unsigned long long tot;
-        const unsigned long long ex = block_exclusive_scan((unsigned long long)keep, sm.ws, tot);
-        if (keep) {
-            const uint32_t w = sm.kept + (uint32_t)ex;
-            hk[w] = key;
-            hv[w] = r;
-            const uint32_t rank = (uint32_t)(key >> 37);
-            const uint32_t rl = a.reads[r];
-            atomicAdd(&sm.nbytes[rank], head_bytes(a.lines[rl >> 1], rl & 1u));
+        if (hc > HEAD_CAP && threadIdx.x == 0) atomicAdd(&a.st->big_head_parts, 1u);
+        for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
+            const uint32_t r = hv[i];
+            const Head h = a.heads[r];
+            hk[i] = head_sort_key(sm.rank_of_slot[h.slot], h.uuid);
         }
         __syncthreads();
+        if (hc <= blockDim.x) {
+            // few heads (the usual case): each thread places its own by counting the smaller
+            // (key, read) pairs; read ordinals are distinct, so the ranks are too
+            unsigned long long mk = 0;
+            uint32_t mv = 0, rank = 0;
+            if (threadIdx.x < hc) {
+                mk = hk[threadIdx.x];
+                mv = hv[threadIdx.x];
+                for (uint32_t j = 0; j < hc; j++) {
+                    const unsigned long long kj = hk[j];
+                    const uint32_t vj = hv[j];
+                    rank += (kj < mk || (kj == mk && vj < mv)) ? 1u : 0u;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x < hc) {
+                hk[rank] = mk;
+                hv[rank] = mv;
+            }
+            __syncthreads();
+        } else {
+            bitonic_sort_pairs<unsigned long long, uint32_t>(hk, hv, hc);
+        }
         if (threadIdx.x == 0) {
-            sm.kept += (uint32_t)tot;
-            sm.carry = last;
+            sm.kept = 0;
+            sm.carry = 0;
         }
         __syncthreads();
+        for (uint32_t c0 = 0; c0 < hc; c0 += blockDim.x) {
+            const uint32_t i = c0 + threadIdx.x;
+            unsigned long long key = 0;
+            uint32_t keep = 0, r = 0;
+            if (i < hc) {
+                key = hk[i];
+                const unsigned long long prev = i == 0 ? ~0ULL : (i == c0 ? sm.carry : hk[i - 1]);
+                keep = key != prev ? 1u : 0u;
+                r = hv[i];
+            }
+            const unsigned long long last = hk[min(hc, c0 + blockDim.x) - 1];
+            unsigned long long tot;
+            const unsigned long long ex = block_exclusive_scan((unsigned long long)keep, sm.ws, tot);
+            if (keep) {
+                const uint32_t w = sm.kept + (uint32_t)ex;
+                hk[w] = key;
+                hv[w] = r;
+                const uint32_t rank = (uint32_t)(key >> 37);
+                const uint32_t rl = a.reads[r];
+                atomicAdd(&sm.nbytes[rank], head_bytes(a.lines[rl >> 1], rl & 1u));
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                sm.kept += (uint32_t)tot;
+                sm.carry = last;
+            }
+            __syncthreads();
+        }
     }
     const uint32_t kept = sm.kept;
     // 6. record offsets of the nodes in the partition
@@ -2194,61 +2238,101 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
     //    set headers, the heads of the node before it
     HeadOut *hout = a.hout + hb;
     const uint32_t keylen = 4 + nb;
-    unsigned long long hrun = 0;
-    for (uint32_t c0 = 0; c0 < kept; c0 += blockDim.x) {
-        const uint32_t i = c0 + threadIdx.x;
-        uint32_t hsz = 0, r = 0, rl = 0;
-        LineRec lr{};
-        if (i < kept) {
-            r = hv[i];
-            rl = a.reads[r];
-            lr = a.lines[rl >> 1];
-            hsz = head_bytes(lr, rl & 1u);
+    if (warp_heads) {
+        if (threadIdx.x < 32) {
+            uint32_t hsz = 0, rl = 0;
+            LineRec lr{};
+            if (wkeep) {
+                rl = a.reads[wv];
+                lr = a.lines[rl >> 1];
+                hsz = head_bytes(lr, rl & 1u);
+            }
+            const uint32_t pre = warp_inclusive_scan(hsz) - hsz;  // bytes of the kept heads before
+            const uint32_t rank = (uint32_t)(wk >> 37);
+            const bool flipped = (wk >> 36) & 1ULL;
+            // the node's kept lanes, its flipped ones, its first lane
+            const uint32_t node_mask = __match_any_sync(0xffffffffu, wkeep ? rank : 0xffffffffu) & wkeep_mask;
+            const uint32_t flip_mask = __ballot_sync(0xffffffffu, wkeep && flipped);
+            const int first = node_mask ? __ffs(node_mask) - 1 : 0;
+            const uint32_t pre0 = __shfl_sync(0xffffffffu, pre, first);
+            if (wkeep) {
+                const uint32_t cu = __popc(node_mask & ~flip_mask), cf = __popc(node_mask & flip_mask);
+                const uint32_t meta = sm.meta[sm.ord[rank]];
+                uint32_t edges = 0;
+                for (int t = 0; t < 4; t++) {
+                    const uint32_t m = (meta >> (4 * t)) & 15u;
+                    if (m) edges += 4 + __popc(m) * (4 + nb);
+                }
+                const uint32_t st = __popc(wkeep_mask & ((1u << first) - 1u));  // kept index of the node's first
+                const uint32_t mate = rl & 1u;
+                HeadOut ho;
+                ho.uuid = a.heads[wv].uuid;
+                ho.s_off = mate ? lr.s1 : lr.s0;
+                ho.m_off = mate ? lr.s0 : lr.s1;
+                ho.L = mate ? lr.l1 : lr.l0;
+                ho.Lm = mate ? lr.l0 : lr.l1;
+                ho.pos = sm.nbytes[rank] + 8 + keylen + 1 + edges + 5 + ((flipped && cu > 0) ? 5 : 0) + (pre - pre0);
+                ho.set_count = (wkept_idx == st && !flipped) ? cu : ((flipped && wkept_idx == st + cu) ? cf : 0u);
+                hout[wkept_idx] = ho;
+            }
         }
-        unsigned long long tot;
-        const unsigned long long ex = block_exclusive_scan((unsigned long long)hsz, sm.ws, tot);
-        // the running byte count of kept heads: stash each head's prefix in hk's low bits
-        if (i < kept) {
-            const unsigned long long pre = hrun + ex;
+    } else {
+        unsigned long long hrun = 0;
+        for (uint32_t c0 = 0; c0 < kept; c0 += blockDim.x) {
+            const uint32_t i = c0 + threadIdx.x;
+            uint32_t hsz = 0, r = 0, rl = 0;
+            LineRec lr{};
+            if (i < kept) {
+                r = hv[i];
+                rl = a.reads[r];
+                lr = a.lines[rl >> 1];
+                hsz = head_bytes(lr, rl & 1u);
+            }
+            unsigned long long tot;
+            const unsigned long long ex = block_exclusive_scan((unsigned long long)hsz, sm.ws, tot);
+            // the running byte count of kept heads: stash each head's prefix in hk's low bits
+            if (i < kept) {
+                const unsigned long long pre = hrun + ex;
+                const unsigned long long key = hk[i];
+                hk[i] = (key & ~((1ULL << 36) - 1)) | pre;  // rank << 37 | flipped << 36 | prefix
+            }
+            hrun += tot;
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
             const unsigned long long key = hk[i];
-            hk[i] = (key & ~((1ULL << 36) - 1)) | pre;  // rank << 37 | flipped << 36 | prefix
+            const uint32_t rank = (uint32_t)(key >> 37);
+            const bool flipped = (key >> 36) & 1ULL;
+            // the node's kept heads: [st, st + cu) unflipped, then cf flipped (hk is sorted by
+            // rank, flipped, position)
+            const unsigned long long rbase = (unsigned long long)rank << 37;
+            const uint32_t st = kept_lower_bound(hk, kept, rbase);
+            const uint32_t fl = kept_lower_bound(hk, kept, rbase | (1ULL << 36));
+            const uint32_t cu = fl - st, cf = kept_lower_bound(hk, kept, rbase + (1ULL << 37)) - fl;
+            const unsigned long long pre = key & ((1ULL << 36) - 1);
+            const unsigned long long pre0 = hk[st] & ((1ULL << 36) - 1);
+            const uint32_t meta = sm.meta[sm.ord[rank]];
+            uint32_t edges = 0;
+            for (int t = 0; t < 4; t++) {
+                const uint32_t m = (meta >> (4 * t)) & 15u;
+                if (m) edges += 4 + __popc(m) * (4 + nb);
+            }
+            const uint32_t pos = sm.nbytes[rank] + 8 + keylen + 1 + edges + 5 + ((flipped && cu > 0) ? 5 : 0) +
+                                 (uint32_t)(pre - pre0);
+            const uint32_t r = hv[i];
+            const uint32_t rl = a.reads[r];
+            const LineRec lr = a.lines[rl >> 1];
+            const uint32_t mate = rl & 1u;
+            HeadOut ho;
+            ho.uuid = a.heads[r].uuid;
+            ho.s_off = mate ? lr.s1 : lr.s0;
+            ho.m_off = mate ? lr.s0 : lr.s1;
+            ho.L = mate ? lr.l1 : lr.l0;
+            ho.Lm = mate ? lr.l0 : lr.l1;
+            ho.pos = pos;
+            ho.set_count = (i == st && !flipped) ? cu : ((flipped && i == st + cu) ? cf : 0u);
+            hout[i] = ho;
         }
-        hrun += tot;
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
-        const unsigned long long key = hk[i];
-        const uint32_t rank = (uint32_t)(key >> 37);
-        const bool flipped = (key >> 36) & 1ULL;
-        // the node's kept heads: [st, st + cu) unflipped, then cf flipped (hk is sorted by
-        // rank, flipped, position)
-        const unsigned long long rbase = (unsigned long long)rank << 37;
-        const uint32_t st = kept_lower_bound(hk, kept, rbase);
-        const uint32_t fl = kept_lower_bound(hk, kept, rbase | (1ULL << 36));
-        const uint32_t cu = fl - st, cf = kept_lower_bound(hk, kept, rbase + (1ULL << 37)) - fl;
-        const unsigned long long pre = key & ((1ULL << 36) - 1);
-        const unsigned long long pre0 = hk[st] & ((1ULL << 36) - 1);
-        const uint32_t meta = sm.meta[sm.ord[rank]];
-        uint32_t edges = 0;
-        for (int t = 0; t < 4; t++) {
-            const uint32_t m = (meta >> (4 * t)) & 15u;
-            if (m) edges += 4 + __popc(m) * (4 + nb);
-        }
-        const uint32_t pos = sm.nbytes[rank] + 8 + keylen + 1 + edges + 5 + ((flipped && cu > 0) ? 5 : 0) +
-                             (uint32_t)(pre - pre0);
-        const uint32_t r = hv[i];
-        const uint32_t rl = a.reads[r];
-        const LineRec lr = a.lines[rl >> 1];
-        const uint32_t mate = rl & 1u;
-        HeadOut ho;
-        ho.uuid = a.heads[r].uuid;
-        ho.s_off = mate ? lr.s1 : lr.s0;
-        ho.m_off = mate ? lr.s0 : lr.s1;
-        ho.L = mate ? lr.l1 : lr.l0;
-        ho.Lm = mate ? lr.l0 : lr.l1;
-        ho.pos = pos;
-        ho.set_count = (i == st && !flipped) ? cu : ((flipped && i == st + cu) ? cf : 0u);
-        hout[i] = ho;
     }
     if (threadIdx.x == 0) {
         a.part_nodes[f] = n;
