@@ -2066,11 +2066,12 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
         h.slot = (uint32_t)sl;
         a.heads[r] = h;
     }
-    __syncthreads();
     // 3. order the nodes deterministically: by home slot (the low hash bits that started the
     //    probe), then by key.  A counting sort over the 2048 homes: keys per home (nbytes),
     //    their offsets, then each key's place among the keys of its home, counted back along
-    //    its probe run (the keys of one home all lie between the home and the key's slot)
+    //    its probe run (the keys of one home all lie between the home and the key's slot).
+    //    (The counts only read the finished table, like the head lookups above: no barrier
+    //    between them.)
     for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x)
         if (sm.key1[i] != (K)0) atomicAdd(&sm.nbytes[sm.home[i]], 1u);
     __syncthreads();
@@ -2434,19 +2435,6 @@ __device__ __forceinline__ void put_key(RecAcc &o, K v, int nb) {
     }
 }
 
-template <class K>
-__device__ __forceinline__ void node_neighbors(K key, uint32_t m, int t, int k, K y[4], int &ny) {
-    ny = 0;
-    for (int e = 0; e < 4; e++)
-        if (m & (1u << e)) y[ny++] = edge_neighbor<K>(key, t, e, k);
-    for (int u = 1; u < ny; u++)
-        for (int v = u; v > 0 && y[v] < y[v - 1]; v--) {
-            const K tmp = y[v];
-            y[v] = y[v - 1];
-            y[v - 1] = tmp;
-        }
-}
-
 // a record larger than a window: byte by byte, only the bytes inside the window
 template <class K>
 __device__ __noinline__ void write_record_bytes(const Sink &o, long long st, long long en, K key, uint32_t meta,
@@ -2459,17 +2447,17 @@ __device__ __noinline__ void write_record_bytes(const Sink &o, long long st, lon
     pos += nb;
     o.b(pos++, active);
     for (int t = 0; t < 4; t++) {
-        const uint32_t m = (meta >> (4 * t)) & 15u;
+        uint32_t m = (meta >> (4 * t)) & 15u;
         if (!m) continue;
-        K y[4];
-        int ny;
-        node_neighbors<K>(key, m, t, k, y, ny);
-        o.u32(pos, (uint32_t)ny);
+        o.u32(pos, (uint32_t)__popc(m));
         pos += 4;
-        for (int u = 0; u < ny; u++) {
+        while (m) {
+            const int e = __ffs(m) - 1;
+            m &= m - 1;
+            const K y = edge_neighbor<K>(key, t, e, k);
             o.u32(pos, (uint32_t)k);
             pos += 4;
-            for (int i = 0; i < nb; i++) o.b(pos + i, KeyOps<K>::byte_at(y[u], nb - 1 - i));
+            for (int i = 0; i < nb; i++) o.b(pos + i, KeyOps<K>::byte_at(y, nb - 1 - i));
             pos += nb;
         }
     }
@@ -2631,24 +2619,19 @@ __global__ void __launch_bounds__(WRITER_WARPS * 32, 3) k_emit_write_part(EmitAr
                 o.be32((uint32_t)k);
                 put_key<K>(o, key, nb);
                 o.put(active, 1);
+                // the edge lists in FF, FR, RF, RR order; a list's neighbours in the order of
+                // their extension base (the reference's lists are unordered sets)
                 uint32_t lists = active & 15u;
                 while (lists) {
                     const int t = __ffs(lists) - 1;
                     lists &= lists - 1;
-                    const uint32_t m = (meta >> (4 * t)) & 15u;
-                    const int ny = __popc(m);
-                    o.be32((uint32_t)ny);
-                    if (ny == 1) {
+                    uint32_t m = (meta >> (4 * t)) & 15u;
+                    o.be32((uint32_t)__popc(m));
+                    while (m) {
+                        const int e = __ffs(m) - 1;
+                        m &= m - 1;
                         o.be32((uint32_t)k);
-                        put_key<K>(o, edge_neighbor<K>(key, t, __ffs(m) - 1, k), nb);
-                    } else {
-                        K y[4];
-                        int c;
-                        node_neighbors<K>(key, m, t, k, y, c);
-                        for (int u = 0; u < c; u++) {
-                            o.be32((uint32_t)k);
-                            put_key<K>(o, y[u], nb);
-                        }
+                        put_key<K>(o, edge_neighbor<K>(key, t, e, k), nb);
                     }
                 }
                 if (!heads) {
