@@ -2529,7 +2529,7 @@ __device__ __forceinline__ void window_out(uint8_t *out, const uint8_t *stage, u
 }
 
 template <class K>
-__global__ void __launch_bounds__(WRITER_WARPS * 32, 3) k_emit_write_part(EmitArgs a) {
+__global__ void __launch_bounds__(WRITER_WARPS * 32, sizeof(K) == 8 ? 4 : 3) k_emit_write_part(EmitArgs a) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint8_t *stage = smem_raw + (size_t)warp * (WARP_STAGE + 32);
