@@ -1624,7 +1624,7 @@ template <class K> struct SuperRound {
 };
 
 template <class K>
-__global__ void __launch_bounds__(SC_THREADS) k_scatter_super(const uint8_t *text, unsigned long long n_text,
+__global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_super(const uint8_t *text, unsigned long long n_text,
                                                               const LineRec *lines,
                                                               const uint32_t *reads, uint32_t n_reads, int k,
                                                               SampleMap m, uint32_t S,
@@ -1785,7 +1785,7 @@ struct FineSmem {
 };
 
 template <class K>
-__global__ void __launch_bounds__(256) k_scatter_fine(const K *okey, const uint16_t *obits, const ulonglong2 *chunks,
+__global__ void __launch_bounds__(256, sizeof(K) == 8 ? 3 : 2) k_scatter_fine(const K *okey, const uint16_t *obits, const ulonglong2 *chunks,
                                                       const SuperInfo *sinfo, const unsigned long long *fine_off,
                                                       uint32_t *fine_cur, K *okey2, uint16_t *obits2) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
