@@ -50,6 +50,7 @@ UNIT = "k-mers/s"
 CPU_SAMPLE_PAIRS = 120_000   # cpu_baseline sample (one run)
 REF_STEP_PAIRS = 60_000      # --impl reference: sample per step
 TUNE_PAIRS = 200_000         # autotuner sample: the first pairs of the workload
+LAYOUT_PARTS = 16            # parts of the reference part layout measurement
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_emit_write_part_pe5mbp_k31.md")
 HEADOUT_BYTES = 48           # one HeadOut entry (uuid, two text offsets, position, counts)
 
@@ -384,6 +385,27 @@ def bench_batched(ctx, samples, steps, warmup, local):
                                   "aggregate": got[0]["ms_aggregate"], "write": got[0]["ms_write"]}}
 
 
+def bench_layout(ctx, w, d_text, warmup, pin, parts=LAYOUT_PARTS, reps=3):
+    """The same build written into the reference's part layout (records regrouped by the
+    reference's Kmer partitioner, one extra pass on the device): its cost beside the job's."""
+    import genomix_gb300 as gx
+
+    sts = []
+    for i in range(max(1, warmup // 2) + reps):
+        job = gx.GraphBuildJob(ctx, w.k, out_parts=parts, layout="reference", **pin)
+        job.add_input_device(d_text.data_ptr(), d_text.numel())
+        job.run()
+        if i >= max(1, warmup // 2):
+            sts.append(job.stats())
+        job.close()
+    ms = statistics.mean(s["ms_layout"] for s in sts)
+    rb = sts[0]["record_bytes"]
+    # records read once while indexed and once while copied, written once; 24 B of index per record
+    alg = 3 * rb + 40 * sts[0]["nodes"]
+    return {"parts": parts, "ms_regroup": ms, "ms_build": statistics.mean(s["ms_total"] for s in sts),
+            "record_bytes": rb, "alg_gbs": alg / (ms / 1e3) / 1e9}
+
+
 def config_of(w, n):
     return {"workload": w.name, "genome_bp": w.genome_len, "pairs": w.reads, "read_len": 150, "k": w.k,
             "input_bytes": len(w.text), "parallelism": f"replicas{n}" if n > 1 else "single",
@@ -492,6 +514,9 @@ def run_gb300(args, ws, rank, local):
     ms_e2e = max_over_ranks(ws, ctx.elapsed_ms(2, 3))
     e2e_value = ws * args.steps * kmers / (ms_e2e / 1e3)
 
+    lay = None
+    if not args.no_layout:
+        lay = bench_layout(ctx, w, d_text, args.warmup, pin)
     bat = srv = None
     if samples is not None:
         bat = bench_batched(ctx, samples, args.steps, args.warmup, local)
@@ -545,6 +570,7 @@ def run_gb300(args, ws, rank, local):
         "batched": bat,
         "serving": srv,
         "long_k": lk,
+        "reference_layout": lay,
         "cpu_baseline": cb,
     }
     print(json.dumps(line), flush=True)
@@ -565,6 +591,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the served-stream measurement")
     ap.add_argument("--no-autotune", action="store_true", help="run with the built-in settings")
     ap.add_argument("--no-long-k", action="store_true", help="skip the 50 Mbp k = 55 measurement")
+    ap.add_argument("--no-layout", action="store_true", help="skip the reference part layout measurement")
     ap.add_argument("--fill", type=float, default=0.0,
                     help="partitioned build at this bucket fill instead of the autotuner's choice (profiling runs)")
     ap.add_argument("--max-pairs", type=int, default=None,

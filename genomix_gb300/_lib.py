@@ -19,6 +19,7 @@ STATUS_NAMES = {
 INPUT_READID, INPUT_FASTQ = 0, 1
 ALGO_DEFAULT, ALGO_PARTITIONED, ALGO_TABLE = 0, 1, 2
 PLAN_BUILD_DEBRUIJN_GRAPH, PLAN_BUILD_READ_PARSER = 0, 1
+LAYOUT_BUCKETS, LAYOUT_REFERENCE_PARTS = 0, 1
 
 # every symbol include/gxgpu.h declares
 EXPORTS = [
@@ -49,8 +50,9 @@ class JobOpts(ctypes.Structure):
         ("threads_per_read", ctypes.c_int),
         ("est_input_bytes", ctypes.c_size_t),
         ("algorithm", ctypes.c_int),
-            ("plan", ctypes.c_int),
-]
+        ("plan", ctypes.c_int),
+        ("layout", ctypes.c_int),
+    ]
 
 
 class ServeOpts(ctypes.Structure):
@@ -125,7 +127,7 @@ class Stats(ctypes.Structure):
         ("kernel_launches", ctypes.c_uint64),
         ("ms_parse", ctypes.c_double), ("ms_insert", ctypes.c_double), ("ms_emit", ctypes.c_double),
         ("ms_total", ctypes.c_double), ("ms_aggregate", ctypes.c_double), ("ms_write", ctypes.c_double),
-        ("attempts", ctypes.c_uint64),
+        ("attempts", ctypes.c_uint64), ("ms_layout", ctypes.c_double),
     ]
 
     def as_dict(self):

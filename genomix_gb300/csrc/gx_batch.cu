@@ -466,7 +466,8 @@ static gx_status batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses)
             continue;
         }
         resolve_options(j);
-        if (j->eff_algorithm == GX_ALGO_TABLE || j->o.plan != GX_PLAN_BUILD_DEBRUIJN_GRAPH) {
+        if (j->eff_algorithm == GX_ALGO_TABLE || j->o.plan != GX_PLAN_BUILD_DEBRUIJN_GRAPH ||
+            j->o.layout != GX_LAYOUT_BUCKETS) {
             result[j] = run_job_locked(j);
             continue;
         }

@@ -202,12 +202,21 @@ static gx_status job_create_impl(gx_ctx *c, const gx_job_opts *opts, gx_job **ou
     const bool has_plan = opts->struct_size >= offsetof(gx_job_opts, plan) + sizeof(int);
     if (has_plan && opts->plan != GX_PLAN_BUILD_DEBRUIJN_GRAPH && opts->plan != GX_PLAN_BUILD_READ_PARSER)
         return GX_EINVAL;
+    const bool has_layout = opts->struct_size >= offsetof(gx_job_opts, layout) + sizeof(int);
+    if (has_layout) {
+        if (opts->layout != GX_LAYOUT_BUCKETS && opts->layout != GX_LAYOUT_REFERENCE_PARTS) return GX_EINVAL;
+        // the read parser's parts follow its input splits, not a key partitioner
+        if (opts->layout == GX_LAYOUT_REFERENCE_PARTS &&
+            ((has_plan && opts->plan != GX_PLAN_BUILD_DEBRUIJN_GRAPH) || opts->out_parts > 65536))
+            return GX_EINVAL;
+    }
     gx_job *j = new (std::nothrow) gx_job();
     if (!j) return GX_ENOMEM;
     j->ctx = c;
     c->refs.fetch_add(1);
     memcpy(&j->o, opts, std::min(sizeof j->o, opts->struct_size));
     if (!has_plan) j->o.plan = GX_PLAN_BUILD_DEBRUIJN_GRAPH;
+    if (!has_layout) j->o.layout = GX_LAYOUT_BUCKETS;
     if (j->o.out_parts == 0) j->o.out_parts = 1;
     j->k = opts->kmer_length;
     j->wide = j->k > 32 ? 1 : 0;
@@ -450,21 +459,102 @@ struct RunCtx {
     std::vector<uint32_t> scnt, hll;
 };
 
+// Regroups a finished record stream into the reference's parts (GX_LAYOUT_REFERENCE_PARTS):
+// each record's part from its key (KmerPartitionComputerFactory.java:28-52), a stable counting
+// sort of the record indexes by part, the record lengths scanned in the new order, one copy into
+// a new buffer.  On success `outp` and `part_off` are replaced (the old ones freed): the new
+// record groups are every 1024th record, for chunked emits; part_bounds are set.
+static gx_status relayout_reference_parts(RunCtx &rc, uint32_t &nparts, unsigned long long total,
+                                          const std::vector<uint32_t> &pn, uint64_t nn, unsigned long long *&part_off,
+                                          void *&outp) {
+    gx_job *j = rc.j;
+    cudaStream_t s = rc.s;
+    const uint32_t P = (uint32_t)j->o.out_parts;
+    if (nn > 0xffffffffULL) return GX_ENOMEM;  // record indexes are 32-bit
+    const uint32_t N = (uint32_t)nn;
+    std::vector<uint32_t> nbase(nparts);
+    uint32_t acc = 0;
+    for (uint32_t q = 0; q < nparts; q++) {
+        nbase[q] = acc;
+        acc += pn[q];
+    }
+    constexpr uint32_t GROUP = 1024;
+    const uint64_t n_groups = (N + GROUP - 1) / GROUP;
+    const uint32_t tiles = rl_tiles(N);
+    const uint64_t ncnt = 256ull * tiles;
+    RunArena ar(s);
+    uint32_t *d_nbase, *rpart, *rlen, *perm, *perm2, *cnt;
+    unsigned long long *roff, *len2, *noff, *bounds;
+    void *scratch;
+    gx_status e;
+    if ((e = ar.alloc(d_nbase, nparts)) != GX_OK) return e;
+    if ((e = ar.alloc(rpart, N)) != GX_OK) return e;
+    if ((e = ar.alloc(rlen, N)) != GX_OK) return e;
+    if ((e = ar.alloc(roff, N)) != GX_OK) return e;
+    if ((e = ar.alloc(perm, N)) != GX_OK) return e;
+    if ((e = ar.alloc(perm2, P > 256 ? N : 1)) != GX_OK) return e;
+    if ((e = ar.alloc(cnt, ncnt)) != GX_OK) return e;
+    if ((e = ar.alloc(len2, N)) != GX_OK) return e;
+    if ((e = ar.alloc(noff, (uint64_t)N + 1)) != GX_OK) return e;
+    if ((e = ar.alloc(bounds, P + 1)) != GX_OK) return e;
+    if ((e = ar.alloc(scratch, std::max(scan_scratch_bytes(ncnt, 8), scan_scratch_bytes((uint64_t)N + 1, 8)))) !=
+        GX_OK)
+        return e;
+    void *nout = nullptr;
+    unsigned long long *groups = nullptr;
+    if (cudaMallocAsync(&nout, total + 16, s) != cudaSuccess) {
+        cudaGetLastError();
+        return GX_ENOMEM;
+    }
+    if (cudaMallocAsync(&groups, (n_groups + 1) * sizeof(unsigned long long), s) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFreeAsync(nout, s);
+        return GX_ENOMEM;
+    }
+    CK(cudaMemcpyAsync(d_nbase, nbase.data(), nparts * 4ull, cudaMemcpyHostToDevice, s));
+    CK(cudaEventRecord(j->tm.ev[7], s));
+    launch_rl_index((const uint8_t *)outp, part_off, d_nbase, nparts, P, rpart, roff, rlen, s);
+    const uint32_t *order = nullptr;
+    uint32_t *dst = perm;
+    for (int shift = 0; shift < (P > 256 ? 16 : 8); shift += 8) {
+        launch_rl_count(rpart, order, N, shift, cnt, s);
+        exclusive_scan_u32(cnt, cnt, ncnt, nullptr, scratch, s);
+        launch_rl_scatter(rpart, order, N, shift, cnt, dst, s);
+        order = dst;
+        dst = dst == perm ? perm2 : perm;
+    }
+    launch_rl_gather_len(order, rlen, N, len2, s);
+    exclusive_scan_u64(len2, noff, N, noff + N, scratch, s);
+    launch_rl_copy((const uint8_t *)outp, order, roff, noff, rlen, N, (uint8_t *)nout, s);
+    launch_rl_bounds(rpart, order, N, P, noff, bounds, s);
+    launch_rl_sample(noff, N, GROUP, n_groups + 1, groups, s);
+    CK(cudaEventRecord(j->tm.ev[8], s));
+    std::vector<unsigned long long> hb(P + 1);
+    unsigned long long moved = 0;
+    CK(d2h_async(hb.data(), bounds, (P + 1) * 8ull, s));
+    CK(d2h_async(&moved, noff + N, 8, s));
+    CK(sync_stream(s));
+    CK(cudaGetLastError());
+    if (moved != total || hb[0] != 0 || hb[P] != total) {
+        cudaFreeAsync(nout, s);
+        cudaFreeAsync(groups, s);
+        fprintf(stderr, "gxgpu: internal error: the regrouped records do not add up\n");
+        return GX_ECUDA;
+    }
+    for (uint32_t q = 0; q <= P; q++) j->part_bounds[q] = hb[q];
+    j->st.ms_layout = j->tm.ms(7, 8);
+    cudaFreeAsync(outp, s);
+    cudaFreeAsync(part_off, s);
+    outp = nout;
+    part_off = groups;
+    nparts = (uint32_t)n_groups;
+    return GX_OK;
+}
+
 static gx_status finish_outputs(RunCtx &rc, uint32_t nparts, unsigned long long total, unsigned long long *part_off,
                                 const uint32_t *part_nodes, const uint32_t *head_cnt2, void *outp) {
     gx_job *j = rc.j;
     const int P = j->o.out_parts;
-    for (int q = 0; q <= P; q++) {
-        const uint64_t tp = (uint64_t)nparts * q / P;
-        unsigned long long v = 0;
-        if (q == P)
-            v = total;
-        else if (tp > 0)
-            CK(d2h_async(&v, part_off + tp, 8, rc.s));
-        CK(sync_stream(rc.s));
-        j->part_bounds[q] = v;
-    }
-    for (int q = 0; q < P; q++) j->cursor[q] = j->part_bounds[q];
     std::vector<uint32_t> pn(nparts), hc(nparts);
     CK(d2h_async(pn.data(), part_nodes, nparts * 4ull, rc.s));
     CK(d2h_async(hc.data(), head_cnt2, nparts * 4ull, rc.s));
@@ -474,6 +564,26 @@ static gx_status finish_outputs(RunCtx &rc, uint32_t nparts, unsigned long long 
         nn += pn[q];
         nh += hc[q];
     }
+    if (j->o.layout == GX_LAYOUT_REFERENCE_PARTS && P > 1 && nn > 0) {
+        const gx_status e = relayout_reference_parts(rc, nparts, total, pn, nn, part_off, outp);
+        if (e != GX_OK) {
+            cudaFreeAsync(outp, rc.s);
+            cudaFreeAsync(part_off, rc.s);
+            return e;
+        }
+    } else {
+        for (int q = 0; q <= P; q++) {
+            const uint64_t tp = (uint64_t)nparts * q / P;
+            unsigned long long v = 0;
+            if (q == P)
+                v = total;
+            else if (tp > 0)
+                CK(d2h_async(&v, part_off + tp, 8, rc.s));
+            CK(sync_stream(rc.s));
+            j->part_bounds[q] = v;
+        }
+    }
+    for (int q = 0; q < P; q++) j->cursor[q] = j->part_bounds[q];
     j->st.nodes = nn;
     j->st.read_heads = nh;
     j->d_out = (uint8_t *)outp;

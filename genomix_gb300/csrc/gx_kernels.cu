@@ -2793,4 +2793,178 @@ void launch_rp_write(int wide, const uint8_t *text, uint64_t n_text, const LineR
 }
 
 
+// ---- the reference's part layout ----------------------------------------------------------------
+// KmerNodePairSequenceWriterFactory writes each record into the part the Hyracks partitioner
+// picked for its key: KmerPartitionComputerFactory.java:28-52, hash = 31 * hash + (signed)
+// byte over the Kmer's packed bytes, sign-folded, modulo the part count.  Regrouping a finished
+// record stream that way: each record's part, a stable counting sort of the record indexes by
+// part (8-bit digits, one or two passes), a scan of the lengths in the new order, and a copy.
+__device__ __forceinline__ uint32_t java_kmer_part(const uint8_t *b, int len, uint32_t nparts) {
+    int32_t h = 1;
+    for (int i = 0; i < len; i++) h = (int32_t)(31u * (uint32_t)h + (uint32_t)(int32_t)(int8_t)b[i]);
+    if (h < 0) h = -(h + 1);
+    return (uint32_t)h % nparts;
+}
+
+__device__ __forceinline__ uint32_t rd_be32_dev(const uint8_t *p) {
+    return ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | p[3];
+}
+
+// one thread per table partition walks its records: part, offset and length of each
+__global__ void k_rl_index(const uint8_t *rec, const unsigned long long *seg, const uint32_t *node_base,
+                           uint32_t n_seg, uint32_t nparts, uint32_t *rpart, unsigned long long *roff,
+                           uint32_t *rlen) {
+    const uint32_t sg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sg >= n_seg) return;
+    unsigned long long p = seg[sg];
+    uint32_t idx = node_base[sg];
+    const unsigned long long e = seg[sg + 1];
+    while (p < e) {
+        const uint8_t *r = rec + p;
+        const uint32_t rl = rd_be32_dev(r), kl = rd_be32_dev(r + 4);
+        rpart[idx] = java_kmer_part(r + 12, (int)kl - 4, nparts);  // the VKmer's packed bytes
+        roff[idx] = p;
+        rlen[idx] = 8 + rl;
+        idx++;
+        p += 8ull + rl;
+    }
+}
+
+constexpr int RL_TILE = 4096;  // records per block in the counting passes
+
+// per tile, how many of its records fall in each digit (column-major: [digit][tile])
+__global__ void __launch_bounds__(256) k_rl_count(const uint32_t *key, const uint32_t *val, uint64_t n, int shift,
+                                                  uint32_t n_tiles, uint32_t *cnt) {
+    __shared__ uint32_t bins[256];
+    bins[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t t0 = (uint64_t)blockIdx.x * RL_TILE;
+    for (uint64_t i = t0 + threadIdx.x; i < min(n, t0 + RL_TILE); i += 256)
+        atomicAdd(&bins[(key[val ? val[i] : i] >> shift) & 255u], 1u);
+    __syncthreads();
+    cnt[(uint64_t)threadIdx.x * n_tiles + blockIdx.x] = bins[threadIdx.x];
+}
+
+// stable scatter: the tile's records in order, 256 at a time; a record's rank among the same
+// digit = earlier rounds + earlier warps of this round + earlier lanes of its warp
+__global__ void __launch_bounds__(256) k_rl_scatter(const uint32_t *key, const uint32_t *val, uint64_t n, int shift,
+                                                    uint32_t n_tiles, const uint32_t *off, uint32_t *out_val) {
+    __shared__ uint32_t run[256];
+    __shared__ uint32_t wcnt[8][256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    run[threadIdx.x] = off[(uint64_t)threadIdx.x * n_tiles + blockIdx.x];
+    const uint64_t t0 = (uint64_t)blockIdx.x * RL_TILE;
+    for (int r = 0; r < RL_TILE / 256; r++) {
+        for (int w = 0; w < 8; w++) wcnt[w][threadIdx.x] = 0;
+        __syncthreads();
+        const uint64_t i = t0 + (uint64_t)r * 256 + threadIdx.x;
+        const bool live = i < n;
+        const uint32_t v = live ? (val ? val[i] : (uint32_t)i) : 0u;
+        const uint32_t d = live ? (key[v] >> shift) & 255u : 256u + lane;  // idle lanes never match
+        const uint32_t same = __match_any_sync(0xffffffffu, d);
+        const uint32_t wr = __popc(same & ((1u << lane) - 1u));
+        if (live && wr == 0) wcnt[warp][d] = __popc(same);
+        __syncthreads();
+        if (live) {
+            uint32_t before = run[d] + wr;
+            for (int w = 0; w < warp; w++) before += wcnt[w][d];
+            out_val[before] = v;
+        }
+        __syncthreads();
+        uint32_t add = 0;
+        for (int w = 0; w < 8; w++) add += wcnt[w][threadIdx.x];
+        run[threadIdx.x] += add;
+        __syncthreads();
+    }
+}
+
+__global__ void k_rl_gather_len(const uint32_t *perm, const uint32_t *rlen, uint64_t n, unsigned long long *len2) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) len2[i] = rlen[perm[i]];
+}
+
+// one warp per record: its bytes to their new place
+__global__ void k_rl_copy(const uint8_t *src, const uint32_t *perm, const unsigned long long *roff,
+                          const unsigned long long *noff, const uint32_t *rlen, uint64_t n, uint8_t *dst) {
+    const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const uint32_t o = perm[i], len = rlen[o];
+    const uint8_t *s = src + roff[o];
+    uint8_t *d = dst + noff[i];
+    for (uint32_t x = lane; x < len; x += 32) d[x] = s[x];
+}
+
+// the first sorted record of each part (empty parts start where the next one does) and the
+// byte offset it lands at; then every stride-th record's offset (emit split points)
+__global__ void k_rl_bounds(const uint32_t *rpart, const uint32_t *perm, uint64_t n, uint32_t nparts,
+                            const unsigned long long *noff, unsigned long long *bounds) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t p = rpart[perm[i]];
+    const uint32_t q0 = i == 0 ? 0u : rpart[perm[i - 1]] + 1u;
+    for (uint32_t q = q0; q <= p; q++) bounds[q] = noff[i];
+    if (i == n - 1)
+        for (uint32_t q = p + 1; q <= nparts; q++) bounds[q] = noff[n];
+}
+
+__global__ void k_rl_sample(const unsigned long long *noff, uint64_t n, uint32_t stride, uint64_t m,
+                            unsigned long long *out) {
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < m) out[g] = noff[min(n, g * stride)];
+}
+
+void launch_rl_bounds(const uint32_t *rpart, const uint32_t *perm, uint64_t n, uint32_t nparts,
+                      const unsigned long long *noff, unsigned long long *bounds, cudaStream_t s) {
+    if (!n) return;
+    t_launches++;
+    k_rl_bounds<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rpart, perm, n, nparts, noff, bounds);
+}
+
+void launch_rl_sample(const unsigned long long *noff, uint64_t n, uint32_t stride, uint64_t m,
+                      unsigned long long *out, cudaStream_t s) {
+    if (!m) return;
+    t_launches++;
+    k_rl_sample<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(noff, n, stride, m, out);
+}
+
+void launch_rl_index(const uint8_t *rec, const unsigned long long *seg, const uint32_t *node_base,
+                     uint32_t n_seg, uint32_t nparts, uint32_t *rpart, unsigned long long *roff, uint32_t *rlen,
+                     cudaStream_t s) {
+    if (!n_seg) return;
+    t_launches++;
+    k_rl_index<<<(n_seg + 127) / 128, 128, 0, s>>>(rec, seg, node_base, n_seg, nparts, rpart, roff, rlen);
+}
+
+uint32_t rl_tiles(uint64_t n) { return (uint32_t)((n + RL_TILE - 1) / RL_TILE); }
+
+void launch_rl_count(const uint32_t *key, const uint32_t *val, uint64_t n, int shift, uint32_t *cnt, cudaStream_t s) {
+    const uint32_t t = rl_tiles(n);
+    if (!t) return;
+    t_launches++;
+    k_rl_count<<<t, 256, 0, s>>>(key, val, n, shift, t, cnt);
+}
+
+void launch_rl_scatter(const uint32_t *key, const uint32_t *val, uint64_t n, int shift, const uint32_t *off,
+                       uint32_t *out_val, cudaStream_t s) {
+    const uint32_t t = rl_tiles(n);
+    if (!t) return;
+    t_launches++;
+    k_rl_scatter<<<t, 256, 0, s>>>(key, val, n, shift, t, off, out_val);
+}
+
+void launch_rl_gather_len(const uint32_t *perm, const uint32_t *rlen, uint64_t n, unsigned long long *len2,
+                          cudaStream_t s) {
+    if (!n) return;
+    t_launches++;
+    k_rl_gather_len<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(perm, rlen, n, len2);
+}
+
+void launch_rl_copy(const uint8_t *src, const uint32_t *perm, const unsigned long long *roff,
+                    const unsigned long long *noff, const uint32_t *rlen, uint64_t n, uint8_t *dst, cudaStream_t s) {
+    if (!n) return;
+    t_launches++;
+    k_rl_copy<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(src, perm, roff, noff, rlen, n, dst);
+}
+
 }  // namespace gx

@@ -183,6 +183,25 @@ struct AggArgs {
 };
 void launch_aggregate(const AggArgs &a, cudaStream_t s);
 
+// the reference's part layout: each record's part (Java 31-hash of its key, modulo nparts),
+// a stable counting sort of record indexes by part (8-bit digits at `shift`; val NULL means
+// the identity), lengths in the new order, and the copy
+void launch_rl_index(const uint8_t *rec, const unsigned long long *seg, const uint32_t *node_base,
+                     uint32_t n_seg, uint32_t nparts, uint32_t *rpart, unsigned long long *roff, uint32_t *rlen,
+                     cudaStream_t s);
+uint32_t rl_tiles(uint64_t n);
+void launch_rl_count(const uint32_t *key, const uint32_t *val, uint64_t n, int shift, uint32_t *cnt, cudaStream_t s);
+void launch_rl_scatter(const uint32_t *key, const uint32_t *val, uint64_t n, int shift, const uint32_t *off,
+                       uint32_t *out_val, cudaStream_t s);
+void launch_rl_gather_len(const uint32_t *perm, const uint32_t *rlen, uint64_t n, unsigned long long *len2,
+                          cudaStream_t s);
+void launch_rl_copy(const uint8_t *src, const uint32_t *perm, const unsigned long long *roff,
+                    const unsigned long long *noff, const uint32_t *rlen, uint64_t n, uint8_t *dst, cudaStream_t s);
+void launch_rl_bounds(const uint32_t *rpart, const uint32_t *perm, uint64_t n, uint32_t nparts,
+                      const unsigned long long *noff, unsigned long long *bounds, cudaStream_t s);
+void launch_rl_sample(const unsigned long long *noff, uint64_t n, uint32_t stride, uint64_t m,
+                      unsigned long long *out, cudaStream_t s);
+
 // FASTQ -> readid on the device: each record's trimmed sequence line(s) and output length,
 // then the readid lines at their scanned offsets
 struct FqRec {

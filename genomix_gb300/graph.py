@@ -144,11 +144,16 @@ class Context:
 
 
 class GraphBuildJob:
-    """One graph build: inputs -> run() -> (VKmer, Node) records."""
+    """One graph build: inputs -> run() -> (VKmer, Node) records.
+
+    layout="buckets" splits the records into out_parts contiguous ranges of hash buckets;
+    layout="reference" puts each record in the part the reference's Kmer partitioner picks
+    (KmerPartitionComputerFactory.java:28-52), so part q holds the record set of the
+    reference's part q (the order within a part is the build's own)."""
 
     def __init__(self, ctx, kmer_length, input_kind="readid", paired=False, out_parts=1, load_factor=0.0,
                  max_readids_per_edge=250, threads_per_read=0, est_input_bytes=0, algorithm="default",
-                 plan="BUILD_DEBRUIJN_GRAPH"):
+                 plan="BUILD_DEBRUIJN_GRAPH", layout="buckets"):
         self.ctx = ctx
         self._L = ctx._L
         kind = {"readid": _lib.INPUT_READID, "fastq": _lib.INPUT_FASTQ}[input_kind]
@@ -156,8 +161,9 @@ class GraphBuildJob:
         pl = {"BUILD_DEBRUIJN_GRAPH": _lib.PLAN_BUILD_DEBRUIJN_GRAPH, "BUILD_READ_PARSER": _lib.PLAN_BUILD_READ_PARSER}[plan]
         o = _lib.JobOpts(ctypes.sizeof(_lib.JobOpts), int(kmer_length), kind, 1 if paired else 0, int(out_parts),
                          float(load_factor), int(max_readids_per_edge), int(threads_per_read), int(est_input_bytes),
-                         algo, pl)
+                         algo, pl, {"buckets": _lib.LAYOUT_BUCKETS, "reference": _lib.LAYOUT_REFERENCE_PARTS}[layout])
         self.plan = plan
+        self.layout = layout
         h = ctypes.c_void_p()
         _check(self._L.gx_job_create(ctx.h, ctypes.byref(o), ctypes.byref(h)), "gx_job_create")
         self.h = h.value
@@ -432,9 +438,12 @@ class GenomixGpuDriver:
     BUILD_DEBRUIJN_GRAPH = "BUILD_DEBRUIJN_GRAPH"
     BUILD_READ_PARSER = "BUILD_READ_PARSER"
 
-    def __init__(self, device=0, threads_per_machine=1):
+    def __init__(self, device=0, threads_per_machine=1, layout="reference"):
+        """layout="reference" (the default) writes the graph plan's part files with the record
+        sets of the reference's part files; "buckets" skips that regrouping pass."""
         self.ctx = Context(device)
         self.threads_per_machine = threads_per_machine
+        self.layout = layout
 
     def run_job(self, conf, plan=BUILD_DEBRUIJN_GRAPH, profile=False):
         """Reads the readid (or FASTQ) inputs named in conf, writes part-N SequenceFiles under
@@ -446,17 +455,18 @@ class GenomixGpuDriver:
         parts = int(conf.get(THREADS_PER_MACHINE, self.threads_per_machine))
         fastq_pe = conf.get(PAIRED_END_FASTQ_INPUTS)
         fastq_se = conf.get(SINGLE_END_FASTQ_INPUTS)
+        lay = dict(plan=plan, layout=self.layout if plan == self.BUILD_DEBRUIJN_GRAPH else "buckets")
         jobs = []
         if fastq_pe or fastq_se:
             if fastq_pe:
                 fs = fastq_pe.split(",")
-                job = GraphBuildJob(self.ctx, k, "fastq", paired=True, out_parts=parts, plan=plan)
+                job = GraphBuildJob(self.ctx, k, "fastq", paired=True, out_parts=parts, **lay)
                 for a, b in zip(fs[0::2], fs[1::2]):
                     job.add_input(open(a, "rb").read(), 0)
                     job.add_input(open(b, "rb").read(), 1)
                 jobs.append(job)
             if fastq_se:
-                job = GraphBuildJob(self.ctx, k, "fastq", paired=False, out_parts=parts, plan=plan)
+                job = GraphBuildJob(self.ctx, k, "fastq", paired=False, out_parts=parts, **lay)
                 for a in fastq_se.split(","):
                     job.add_input(open(a, "rb").read(), 0)
                 jobs.append(job)
@@ -469,11 +479,11 @@ class GenomixGpuDriver:
                     text += fastq_to_readid(open(a, "rb").read())
                 for j in jobs:
                     j.close()
-                job = GraphBuildJob(self.ctx, k, "readid", out_parts=parts, plan=plan)
+                job = GraphBuildJob(self.ctx, k, "readid", out_parts=parts, **lay)
                 job.add_input(text)
                 jobs = [job]
         else:
-            job = GraphBuildJob(self.ctx, k, "readid", out_parts=parts, plan=plan)
+            job = GraphBuildJob(self.ctx, k, "readid", out_parts=parts, **lay)
             for f in _input_files(conf[INPUT_DIR].split(",")):
                 with open(f, "rb") as fh:
                     job.add_input(fh.read())

@@ -93,7 +93,22 @@ typedef struct gx_job_opts {
     size_t est_input_bytes;   /* capacity hint for the device input buffer; 0 = grow on demand */
     int algorithm;            /* GX_ALGO_*: how occurrences are aggregated */
     int plan;                 /* GX_PLAN_*: what the job writes */
+    int layout;               /* GX_LAYOUT_*: which records go to which output part */
 } gx_job_opts;
+
+/* Output part layouts (gx_job_opts.layout); the records are the same in both, only their
+   grouping into parts differs. */
+enum {
+    GX_LAYOUT_BUCKETS = 0,         /* part q = a contiguous range of the build's hash buckets
+                                      (no extra pass) */
+    GX_LAYOUT_REFERENCE_PARTS = 1  /* part q = the records whose key the reference's partitioner
+                                      sends to part q (KmerPartitionComputerFactory.java:28-52:
+                                      31-hash of the packed k-mer bytes, sign-folded, mod parts),
+                                      so part files hold the same record sets as the reference's
+                                      part-NNNNN files; within a part the order is the build's.
+                                      Graph plan only; out_parts <= 65536.  Costs a regrouping
+                                      pass over the records and a second record buffer. */
+};
 
 /* Plans (gx_job_opts.plan), GenomixHyracksDriver.Plan (GenomixHyracksDriver.java:55-60). */
 enum {
@@ -131,6 +146,8 @@ typedef struct gx_stats {
     double ms_aggregate;      /* device time of the per-bucket aggregation (part of ms_emit) */
     double ms_write;          /* device time of the record-writer kernel (part of ms_emit) */
     uint64_t attempts;        /* passes run: 1, plus one per table/bucket overflow retried */
+    double ms_layout;         /* device time of the regrouping into the reference's parts
+                                 (GX_LAYOUT_REFERENCE_PARTS; 0 otherwise) */
 } gx_stats;
 
 /* ---- context ------------------------------------------------------------------------- */
