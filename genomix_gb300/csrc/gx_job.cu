@@ -459,84 +459,138 @@ struct RunCtx {
     std::vector<uint32_t> scnt, hll;
 };
 
+// Where the partitioned build keeps its records: node j of bucket p starts noff[node_base[p] + j]
+// bytes into the bucket's records (no walk needed to index them).
+struct NodeRecords {
+    const void *nkey = nullptr;  // node keys, same indexing
+    const uint32_t *noff = nullptr;
+    const unsigned long long *node_base = nullptr;
+};
+
 // Regroups a finished record stream into the reference's parts (GX_LAYOUT_REFERENCE_PARTS):
-// each record's part from its key (KmerPartitionComputerFactory.java:28-52), a stable counting
-// sort of the record indexes by part, the record lengths scanned in the new order, one copy into
-// a new buffer.  On success `outp` and `part_off` are replaced (the old ones freed): the new
-// record groups are every 1024th record, for chunked emits; part_bounds are set.
+// each record's part from its key (KmerPartitionComputerFactory.java:28-52), then a stable
+// regrouping by part into a new buffer.  Up to 256 parts: one pass that moves the records
+// straight to their places (per tile and part, byte counts; their scan; a staged copy), the
+// tiles being the partitioned build's buckets (read from its node keys and offsets) or runs of
+// records indexed by a walk.  More parts: a stable counting sort of record indexes (two 8-bit
+// passes), the lengths scanned in the new order, a gather copy.  On success `outp` and
+// `part_off` are replaced (the old ones freed) by the new records and a sorted list of record
+// boundaries (for chunked emits), and part_bounds are set.
 static gx_status relayout_reference_parts(RunCtx &rc, uint32_t &nparts, unsigned long long total,
-                                          const std::vector<uint32_t> &pn, uint64_t nn, unsigned long long *&part_off,
-                                          void *&outp) {
+                                          const std::vector<uint32_t> &pn, const uint32_t *d_part_nodes, uint64_t nn,
+                                          const NodeRecords *nr, unsigned long long *&part_off, void *&outp) {
     gx_job *j = rc.j;
     cudaStream_t s = rc.s;
     const uint32_t P = (uint32_t)j->o.out_parts;
     if (nn > 0xffffffffULL) return GX_ENOMEM;  // record indexes are 32-bit
     const uint32_t N = (uint32_t)nn;
-    std::vector<uint32_t> nbase(nparts);
-    uint32_t acc = 0;
-    for (uint32_t q = 0; q < nparts; q++) {
-        nbase[q] = acc;
-        acc += pn[q];
-    }
-    constexpr uint32_t GROUP = 1024;
-    const uint64_t n_groups = (N + GROUP - 1) / GROUP;
-    const uint32_t tiles = rl_tiles(N);
-    const uint64_t ncnt = 256ull * tiles;
+    const bool one_pass = P <= 256;
+    const bool by_bucket = one_pass && nr;  // no per-record arrays
     RunArena ar(s);
-    uint32_t *d_nbase, *rpart, *rlen, *perm, *perm2, *cnt;
-    unsigned long long *roff, *len2, *noff, *bounds;
-    void *scratch;
     gx_status e;
-    if ((e = ar.alloc(d_nbase, nparts)) != GX_OK) return e;
-    if ((e = ar.alloc(rpart, N)) != GX_OK) return e;
-    if ((e = ar.alloc(rlen, N)) != GX_OK) return e;
-    if ((e = ar.alloc(roff, N)) != GX_OK) return e;
-    if ((e = ar.alloc(perm, N)) != GX_OK) return e;
-    if ((e = ar.alloc(perm2, P > 256 ? N : 1)) != GX_OK) return e;
-    if ((e = ar.alloc(cnt, ncnt)) != GX_OK) return e;
-    if ((e = ar.alloc(len2, N)) != GX_OK) return e;
-    if ((e = ar.alloc(noff, (uint64_t)N + 1)) != GX_OK) return e;
+    uint32_t *rpart = nullptr, *rlen = nullptr;
+    unsigned long long *roff = nullptr, *bounds;
     if ((e = ar.alloc(bounds, P + 1)) != GX_OK) return e;
-    if ((e = ar.alloc(scratch, std::max(scan_scratch_bytes(ncnt, 8), scan_scratch_bytes((uint64_t)N + 1, 8)))) !=
-        GX_OK)
-        return e;
+    if (!by_bucket) {
+        std::vector<uint32_t> nbase(nparts);
+        uint32_t acc = 0;
+        for (uint32_t q = 0; q < nparts; q++) {
+            nbase[q] = acc;
+            acc += pn[q];
+        }
+        uint32_t *d_nbase;
+        if ((e = ar.alloc(d_nbase, nparts)) != GX_OK) return e;
+        if ((e = ar.alloc(rpart, N)) != GX_OK) return e;
+        if ((e = ar.alloc(rlen, N)) != GX_OK) return e;
+        if ((e = ar.alloc(roff, N)) != GX_OK) return e;
+        CK(cudaMemcpyAsync(d_nbase, nbase.data(), nparts * 4ull, cudaMemcpyHostToDevice, s));
+        CK(sync_stream(s));  // nbase is read by the copy
+        CK(cudaEventRecord(j->tm.ev[7], s));
+        if (nr)
+            launch_rl_index_nodes(nr->nkey, j->wide, j->k, part_off, nr->node_base, nr->noff, d_nbase, d_part_nodes,
+                                  nparts, P, rpart, roff, rlen, s);
+        else
+            launch_rl_index((const uint8_t *)outp, part_off, d_nbase, nparts, P, rpart, roff, rlen, s);
+    } else {
+        CK(cudaEventRecord(j->tm.ev[7], s));
+    }
     void *nout = nullptr;
-    unsigned long long *groups = nullptr;
     if (cudaMallocAsync(&nout, total + 16, s) != cudaSuccess) {
         cudaGetLastError();
         return GX_ENOMEM;
     }
+    struct OutGuard {
+        void *&p;
+        cudaStream_t s;
+        ~OutGuard() {
+            if (p) cudaFreeAsync(p, s);
+        }
+    } guard{nout, s};
+    // the record boundaries of the new layout: every entry of the scanned tile counts, or every
+    // 1024th record; at most ~64K of them are kept
+    const unsigned long long *bnd;
+    uint64_t n_bnd;  // entries of bnd, the last one the total
+    unsigned long long moved = 0;
+    if (one_pass) {
+        const uint32_t tiles = by_bucket ? nparts : rl_tiles(N);
+        const uint64_t ncnt = (uint64_t)P * tiles;
+        unsigned long long *cnt;
+        void *scratch;
+        if ((e = ar.alloc(cnt, ncnt + 1)) != GX_OK) return e;
+        if ((e = ar.alloc(scratch, scan_scratch_bytes(ncnt, 8))) != GX_OK) return e;
+        if (by_bucket)
+            launch_rl_regroup_nodes((const uint8_t *)outp, nr->nkey, j->wide, j->k, nr->noff, nr->node_base, part_off,
+                                    d_part_nodes, nparts, P, cnt, scratch, (uint8_t *)nout, s);
+        else
+            launch_rl_regroup_arrays((const uint8_t *)outp, rpart, rlen, roff, N, P, cnt, scratch, (uint8_t *)nout, s);
+        launch_rl_part_starts(cnt, tiles, P, total, bounds, s);
+        CK(d2h_async(&moved, cnt + ncnt, 8, s));
+        bnd = cnt;
+        n_bnd = ncnt + 1;
+    } else {
+        uint32_t *perm, *perm2, *cnt;
+        unsigned long long *len2, *noff;
+        void *scratch;
+        const uint64_t ncnt = 256ull * rl_tiles(N);
+        if ((e = ar.alloc(perm, N)) != GX_OK) return e;
+        if ((e = ar.alloc(perm2, N)) != GX_OK) return e;
+        if ((e = ar.alloc(cnt, ncnt)) != GX_OK) return e;
+        if ((e = ar.alloc(len2, N)) != GX_OK) return e;
+        if ((e = ar.alloc(noff, (uint64_t)N + 1)) != GX_OK) return e;
+        if ((e = ar.alloc(scratch, std::max(scan_scratch_bytes(ncnt, 8), scan_scratch_bytes((uint64_t)N + 1, 8)))) !=
+            GX_OK)
+            return e;
+        const uint32_t *order = nullptr;
+        uint32_t *dst = perm;
+        for (int shift = 0; shift < 16; shift += 8) {
+            launch_rl_count(rpart, order, N, shift, cnt, s);
+            exclusive_scan_u32(cnt, cnt, ncnt, nullptr, scratch, s);
+            launch_rl_scatter(rpart, order, N, shift, cnt, dst, s);
+            order = dst;
+            dst = dst == perm ? perm2 : perm;
+        }
+        launch_rl_gather_len(order, rlen, N, len2, s);
+        exclusive_scan_u64(len2, noff, N, noff + N, scratch, s);
+        launch_rl_copy((const uint8_t *)outp, order, roff, noff, rlen, N, (uint8_t *)nout, s);
+        launch_rl_bounds(rpart, order, N, P, noff, bounds, s);
+        CK(d2h_async(&moved, noff + N, 8, s));
+        bnd = noff;
+        n_bnd = (uint64_t)N + 1;
+    }
+    const uint64_t stride = std::max<uint64_t>(1, (n_bnd + 65535) / 65536);
+    const uint64_t n_groups = (n_bnd - 1 + stride - 1) / stride;  // the total comes last
+    unsigned long long *groups = nullptr;
     if (cudaMallocAsync(&groups, (n_groups + 1) * sizeof(unsigned long long), s) != cudaSuccess) {
         cudaGetLastError();
-        cudaFreeAsync(nout, s);
         return GX_ENOMEM;
     }
-    CK(cudaMemcpyAsync(d_nbase, nbase.data(), nparts * 4ull, cudaMemcpyHostToDevice, s));
-    CK(cudaEventRecord(j->tm.ev[7], s));
-    launch_rl_index((const uint8_t *)outp, part_off, d_nbase, nparts, P, rpart, roff, rlen, s);
-    const uint32_t *order = nullptr;
-    uint32_t *dst = perm;
-    for (int shift = 0; shift < (P > 256 ? 16 : 8); shift += 8) {
-        launch_rl_count(rpart, order, N, shift, cnt, s);
-        exclusive_scan_u32(cnt, cnt, ncnt, nullptr, scratch, s);
-        launch_rl_scatter(rpart, order, N, shift, cnt, dst, s);
-        order = dst;
-        dst = dst == perm ? perm2 : perm;
-    }
-    launch_rl_gather_len(order, rlen, N, len2, s);
-    exclusive_scan_u64(len2, noff, N, noff + N, scratch, s);
-    launch_rl_copy((const uint8_t *)outp, order, roff, noff, rlen, N, (uint8_t *)nout, s);
-    launch_rl_bounds(rpart, order, N, P, noff, bounds, s);
-    launch_rl_sample(noff, N, GROUP, n_groups + 1, groups, s);
+    launch_rl_sample(bnd, n_bnd - 1, (uint32_t)stride, n_groups + 1, groups, s);
     CK(cudaEventRecord(j->tm.ev[8], s));
     std::vector<unsigned long long> hb(P + 1);
-    unsigned long long moved = 0;
     CK(d2h_async(hb.data(), bounds, (P + 1) * 8ull, s));
-    CK(d2h_async(&moved, noff + N, 8, s));
     CK(sync_stream(s));
     CK(cudaGetLastError());
     if (moved != total || hb[0] != 0 || hb[P] != total) {
-        cudaFreeAsync(nout, s);
         cudaFreeAsync(groups, s);
         fprintf(stderr, "gxgpu: internal error: the regrouped records do not add up\n");
         return GX_ECUDA;
@@ -546,13 +600,15 @@ static gx_status relayout_reference_parts(RunCtx &rc, uint32_t &nparts, unsigned
     cudaFreeAsync(outp, s);
     cudaFreeAsync(part_off, s);
     outp = nout;
+    nout = nullptr;  // the job owns it now: the guard lets go
     part_off = groups;
     nparts = (uint32_t)n_groups;
     return GX_OK;
 }
 
 static gx_status finish_outputs(RunCtx &rc, uint32_t nparts, unsigned long long total, unsigned long long *part_off,
-                                const uint32_t *part_nodes, const uint32_t *head_cnt2, void *outp) {
+                                const uint32_t *part_nodes, const uint32_t *head_cnt2, void *outp,
+                                const NodeRecords *nr = nullptr) {
     gx_job *j = rc.j;
     const int P = j->o.out_parts;
     std::vector<uint32_t> pn(nparts), hc(nparts);
@@ -565,7 +621,7 @@ static gx_status finish_outputs(RunCtx &rc, uint32_t nparts, unsigned long long 
         nh += hc[q];
     }
     if (j->o.layout == GX_LAYOUT_REFERENCE_PARTS && P > 1 && nn > 0) {
-        const gx_status e = relayout_reference_parts(rc, nparts, total, pn, nn, part_off, outp);
+        const gx_status e = relayout_reference_parts(rc, nparts, total, pn, part_nodes, nn, nr, part_off, outp);
         if (e != GX_OK) {
             cudaFreeAsync(outp, rc.s);
             cudaFreeAsync(part_off, rc.s);
@@ -966,7 +1022,11 @@ static gx_status build_partitioned(RunCtx &rc) {
             fprintf(stderr, "gxgpu: internal error: record sizes disagree between emission passes\n");
             return GX_ECUDA;
         }
-        if ((e = finish_outputs(rc, P, total, part_off, part_nodes, head_cnt2, outp)) != GX_OK) return e;
+        NodeRecords nr;
+        nr.nkey = okey2;
+        nr.noff = noff;
+        nr.node_base = fine_off;
+        if ((e = finish_outputs(rc, P, total, part_off, part_nodes, head_cnt2, outp, &nr)) != GX_OK) return e;
         j->st.table_slots = (uint64_t)P * AGG_SLOTS;
         j->st.table_partitions = P;
         j->st.attempts = (uint64_t)attempt + 1;

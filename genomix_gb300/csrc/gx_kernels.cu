@@ -2830,7 +2830,287 @@ __global__ void k_rl_index(const uint8_t *rec, const unsigned long long *seg, co
     }
 }
 
+// partitioned build: the nodes of bucket p sit at node_base[p] .. + part_nodes[p] in nkey (their
+// keys) and noff (their record offsets within the bucket): the part from the key's packed bytes,
+// most significant first as the record holds them; one block per bucket, one thread per record
+template <class K>
+__global__ void k_rl_index_nodes(const K *nkey, const unsigned long long *part_off, const unsigned long long *node_base,
+                                 const uint32_t *noff, const uint32_t *dense_base, const uint32_t *part_nodes,
+                                 uint32_t n_buckets, uint32_t nparts, int nb, uint32_t *rpart,
+                                 unsigned long long *roff, uint32_t *rlen) {
+    for (uint32_t p = blockIdx.x; p < n_buckets; p += gridDim.x) {
+        const uint32_t n = part_nodes[p], db = dense_base[p];
+        const unsigned long long base = part_off[p], end = part_off[p + 1];
+        const uint32_t *no = noff + node_base[p];
+        const K *nk = nkey + node_base[p];
+        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+            const unsigned long long o = base + no[j];
+            const unsigned long long e = j + 1 < n ? base + no[j + 1] : end;
+            const K v = nk[j];
+            int32_t h = 1;
+            for (int i = nb - 1; i >= 0; i--)
+                h = (int32_t)(31u * (uint32_t)h + (uint32_t)(int32_t)(int8_t)KeyOps<K>::byte_at(v, i));
+            if (h < 0) h = -(h + 1);
+            rpart[db + j] = (uint32_t)h % nparts;
+            roff[db + j] = o;
+            rlen[db + j] = (uint32_t)(e - o);
+        }
+    }
+}
+
 constexpr int RL_TILE = 4096;  // records per block in the counting passes
+
+// Up to 256 parts: one stable pass that moves bytes, not indexes.  The records are cut into
+// tiles of consecutive records (a source range without gaps): per tile and part, the part's bytes
+// in the tile ([part][tile]); their exclusive scan is where each tile's run of each part lands,
+// and every entry of it is a record boundary of the new layout.  Two record sources: arrays of
+// (part, length, offset) per record in tiles of RL_TILE, or the partitioned build's buckets as
+// tiles, read straight from its node keys and record offsets.
+struct RecArrays {
+    const uint32_t *rpart, *rlen;
+    const unsigned long long *roff;
+    uint64_t n;
+    __device__ uint32_t tile_size(uint32_t t) const {
+        const uint64_t rem = n - (uint64_t)t * RL_TILE;
+        return rem < (uint64_t)RL_TILE ? (uint32_t)rem : (uint32_t)RL_TILE;
+    }
+    __device__ void get(uint32_t t, uint32_t j, uint32_t, uint32_t &d, uint32_t &len,
+                        unsigned long long &off) const {
+        const uint64_t i = (uint64_t)t * RL_TILE + j;
+        d = rpart[i];
+        len = rlen[i];
+        off = roff[i];
+    }
+};
+
+template <class K>
+struct RecNodes {
+    const K *nkey;
+    const uint32_t *noff;
+    const unsigned long long *node_base, *part_off;
+    const uint32_t *part_nodes;
+    int nb;
+    uint32_t nparts;
+    __device__ uint32_t tile_size(uint32_t t) const { return part_nodes[t]; }
+    __device__ void get(uint32_t t, uint32_t j, uint32_t n, uint32_t &d, uint32_t &len,
+                        unsigned long long &off) const {
+        const unsigned long long nbase = node_base[t], base = part_off[t];
+        off = base + noff[nbase + j];
+        const unsigned long long e = j + 1 < n ? base + noff[nbase + j + 1] : part_off[t + 1];
+        len = (uint32_t)(e - off);
+        const K v = nkey[nbase + j];
+        int32_t h = 1;
+        for (int i = nb - 1; i >= 0; i--)
+            h = (int32_t)(31u * (uint32_t)h + (uint32_t)(int32_t)(int8_t)KeyOps<K>::byte_at(v, i));
+        if (h < 0) h = -(h + 1);
+        d = (uint32_t)h % nparts;
+    }
+};
+
+// per tile, each part's bytes; lanes of one part in a warp add up before one shared atomic
+template <class Src>
+__global__ void __launch_bounds__(256) k_rl_tile_bytes(Src src, uint32_t n_tiles, uint32_t nparts,
+                                                       unsigned long long *cnt) {
+    __shared__ unsigned long long bins[256];
+    __shared__ uint32_t slen[256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        bins[threadIdx.x] = 0;
+        __syncthreads();
+        const uint32_t n = src.tile_size(t);
+        for (uint32_t j0 = 0; j0 < n; j0 += 256) {
+            const uint32_t j = j0 + threadIdx.x;
+            uint32_t d = 256u + lane, len = 0;
+            unsigned long long off;
+            if (j < n) src.get(t, j, n, d, len, off);
+            slen[threadIdx.x] = len;
+            const uint32_t same = __match_any_sync(0xffffffffu, d);
+            __syncwarp();
+            if (j < n && (same & ((1u << lane) - 1u)) == 0) {
+                unsigned long long sum = 0;
+                for (uint32_t m = same; m; m &= m - 1) sum += slen[warp * 32 + __ffs(m) - 1];
+                atomicAdd(&bins[d], sum);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        if (threadIdx.x < nparts) cnt[(uint64_t)threadIdx.x * n_tiles + t] = bins[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+constexpr int RL_STAGE = 36 * 1024;              // source bytes of one round, staged in shared memory
+constexpr int RL_OUT = RL_STAGE + 256 * 16;        // the round's output runs, each at its destination's alignment
+constexpr int RL_SMEM = RL_STAGE + 16 + RL_OUT;    // dynamic shared memory of k_rl_move
+
+// copies n bytes between shared-memory addresses of any alignment: bytes up to the destination's
+// word boundary, then whole destination words assembled from two source words, then the rest
+__device__ __forceinline__ void smem_copy_bytes(uint8_t *d, const uint8_t *s, uint32_t n) {
+    uint32_t i = min(n, (4u - ((uint32_t)(uintptr_t)d & 3u)) & 3u);
+    for (uint32_t x = 0; x < i; x++) d[x] = s[x];
+    const uint32_t nw = (n - i) >> 2;
+    if (nw) {
+        const uint8_t *sp = s + i;
+        const uint32_t sh = ((uint32_t)(uintptr_t)sp & 3u) * 8u;
+        const uint32_t *sw = reinterpret_cast<const uint32_t *>((uintptr_t)sp & ~(uintptr_t)3);
+        uint32_t *dw = reinterpret_cast<uint32_t *>(d + i);
+        uint32_t lo = sw[0];
+        for (uint32_t w = 0; w < nw; w++) {
+            const uint32_t hi = sw[w + 1];
+            dw[w] = __funnelshift_r(lo, hi, sh);
+            lo = hi;
+        }
+        i += nw * 4;
+    }
+    for (; i < n; i++) d[i] = s[i];
+}
+
+// The tile's records in source order, 256 at a time.  A record lands after the earlier records
+// of its part (earlier rounds, earlier warps of this round, earlier lanes of its warp), so this
+// round's records of part d form one run of the output, starting where the part's previous run
+// ended.  The round's source bytes (one range) come in with 16-byte loads; each thread copies
+// its record into that run's image in shared memory, the image placed at the run's own 16-byte
+// alignment; each warp then writes whole runs out with aligned 16-byte stores (the ragged ends
+// byte by byte, one lane per byte).  A round whose range does not fit (a giant record) copies
+// each record from global memory with a warp instead.  The next round's record descriptors and
+// the next tile's part offsets are loaded while the current round works.
+template <class Src>
+__global__ void __launch_bounds__(256) k_rl_move(const uint8_t *sbytes, Src src, uint32_t n_tiles, uint32_t nparts,
+                                                 const unsigned long long *off, uint8_t *dst) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint8_t *stage = smem;                 // RL_STAGE + 16 (word reads may run 3 bytes past a record)
+    uint8_t *img = smem + RL_STAGE + 16;   // RL_OUT
+    __shared__ unsigned long long run[256];
+    __shared__ unsigned long long wb[8][256];
+    __shared__ unsigned long long sdst[256], ssrc[256];
+    __shared__ uint32_t slen[256], obase[256], wsum[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t tid = threadIdx.x;
+    uint32_t t = blockIdx.x;
+    if (t >= n_tiles) return;
+    uint32_t n = src.tile_size(t), j0 = 0;
+    // this round's descriptor (d, len, so) and the tile's offsets, loaded one round ahead
+    uint32_t d = 256u + lane, len = 0;
+    unsigned long long so = 0;
+    if (tid < n) src.get(t, tid, n, d, len, so);
+    run[tid] = tid < nparts ? off[(uint64_t)tid * n_tiles + t] : 0ull;
+    for (;;) {
+        const bool live = j0 + tid < n;
+        for (int w = 0; w < 8; w++) wb[w][tid] = 0;
+        slen[tid] = len;
+        ssrc[tid] = so;
+        __syncthreads();
+        // the next round: the rest of this tile, else the next tile
+        uint32_t nt = t, nj0 = j0 + 256, nn = n;
+        if (nj0 >= n) {
+            nt = t + gridDim.x;
+            nj0 = 0;
+            nn = nt < n_tiles ? src.tile_size(nt) : 0u;
+        }
+        uint32_t d2 = 256u + lane, len2 = 0;
+        unsigned long long so2 = 0, run2 = 0;
+        if (nt < n_tiles && nj0 + tid < nn) src.get(nt, nj0 + tid, nn, d2, len2, so2);
+        if (nt != t && nt < n_tiles && tid < nparts) run2 = off[(uint64_t)tid * n_tiles + nt];
+        // ranks within the warp
+        const uint32_t same = __match_any_sync(0xffffffffu, d);
+        uint32_t pre = 0;
+        for (uint32_t m = same & ((1u << lane) - 1u); m; m &= m - 1) pre += slen[warp * 32 + __ffs(m) - 1];
+        if (live && (same >> lane) == 1u) wb[warp][d] = (unsigned long long)pre + len;  // the group's last lane
+        // the round's source range; its loads go out first
+        const uint32_t cnt = min(256u, n - j0);
+        const unsigned long long lo = ssrc[0] & ~15ull, hi = (ssrc[cnt - 1] + slen[cnt - 1] + 15) & ~15ull;
+        const bool fits = hi - lo <= (unsigned long long)RL_STAGE;
+        if (fits) {
+            const uint32_t span = (uint32_t)(hi - lo);
+            const uint8_t *sb = sbytes + lo;
+            for (uint32_t x = 16u * tid; x < span; x += 16u * 256u)
+                *reinterpret_cast<uint4 *>(stage + x) = *reinterpret_cast<const uint4 *>(sb + x);
+        }
+        __syncthreads();
+        // this thread's part (tid): its run this round and the run's image slot
+        unsigned long long bytes = 0;
+        for (int w = 0; w < 8; w++) bytes += wb[w][tid];
+        const uint32_t g15 = (uint32_t)run[tid] & 15u;
+        const uint32_t res = bytes ? (uint32_t)min((g15 + bytes + 15ull) & ~15ull, (unsigned long long)RL_OUT + 16) : 0u;
+        uint32_t inc = res;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        for (int w = 0; w < 8; w++) {
+            const uint32_t v = wsum[w];
+            before += w < warp ? v : 0u;
+            total += v;
+        }
+        obase[tid] = before + inc - res;
+        const bool staged = fits && total <= (uint32_t)RL_OUT;
+        __syncthreads();
+        if (live) {
+            unsigned long long rank = pre;  // bytes of the part before this record, this round
+            for (int w = 0; w < warp; w++) rank += wb[w][d];
+            if (staged)
+                smem_copy_bytes(img + obase[d] + ((uint32_t)run[d] & 15u) + (uint32_t)rank,
+                                stage + (uint32_t)(so - lo), len);
+            else
+                sdst[tid] = run[d] + rank;
+        }
+        __syncthreads();
+        if (staged) {
+            for (uint32_t q = warp; q < nparts; q += 8) {
+                unsigned long long b = 0;
+                for (int w = 0; w < 8; w++) b += wb[w][q];
+                if (!b) continue;
+                const unsigned long long s0 = run[q];
+                const uint32_t h = (uint32_t)s0 & 15u;                    // image offset of the run's first byte
+                const uint32_t e = h + (uint32_t)b;                        // image offset of its end
+                uint8_t *dq = dst + (s0 & ~15ull);
+                const uint8_t *im = img + obase[q];
+                const uint32_t fe = e & ~15u;                              // whole 16-byte units: [fb, fe)
+                const uint32_t fb = (h + 15u) & ~15u;
+                for (uint32_t u = fb + 16u * lane; u < fe; u += 16u * 32u)
+                    *reinterpret_cast<uint4 *>(dq + u) = *reinterpret_cast<const uint4 *>(im + u);
+                // ragged ends: the head [h, min(fb, e)) and the tail [max(fe, fb), e), one lane per byte
+                const uint32_t hx = h + lane;
+                if (hx < fb && hx < e) dq[hx] = im[hx];
+                const uint32_t tx = max(fe, fb) + lane;
+                if (lane < 16 && tx < e) dq[tx] = im[tx];
+            }
+        } else {
+            for (uint32_t q = 0; q < 32; q++) {
+                const uint32_t r = warp * 32 + q;
+                if (r >= cnt) break;
+                const uint32_t L = slen[r];
+                const uint8_t *sp = sbytes + ssrc[r];
+                uint8_t *dp = dst + sdst[r];
+                for (uint32_t x = lane; x < L; x += 32) dp[x] = sp[x];
+            }
+        }
+        __syncthreads();
+        if (nt >= n_tiles) break;
+        if (nt != t) {
+            run[tid] = run2;
+        } else {
+            run[tid] += bytes;
+        }
+        t = nt;
+        j0 = nj0;
+        n = nn;
+        d = d2;
+        len = len2;
+        so = so2;
+    }
+}
+
+__global__ void k_rl_part_starts(const unsigned long long *off, uint32_t n_tiles, uint32_t nparts,
+                                 unsigned long long total, unsigned long long *bounds) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nparts) bounds[q] = off[(uint64_t)q * n_tiles];
+    if (q == nparts) bounds[q] = total;
+}
 
 // per tile, how many of its records fall in each digit (column-major: [digit][tile])
 __global__ void __launch_bounds__(256) k_rl_count(const uint32_t *key, const uint32_t *val, uint64_t n, int shift,
@@ -2937,6 +3217,64 @@ void launch_rl_index(const uint8_t *rec, const unsigned long long *seg, const ui
 }
 
 uint32_t rl_tiles(uint64_t n) { return (uint32_t)((n + RL_TILE - 1) / RL_TILE); }
+
+void launch_rl_index_nodes(const void *nkey, int wide, int k, const unsigned long long *part_off,
+                           const unsigned long long *node_base, const uint32_t *noff, const uint32_t *dense_base,
+                           const uint32_t *part_nodes, uint32_t n_buckets, uint32_t nparts, uint32_t *rpart,
+                           unsigned long long *roff, uint32_t *rlen, cudaStream_t s) {
+    if (!n_buckets) return;
+    t_launches++;
+    const unsigned blocks = std::min<uint32_t>(n_buckets, 152u * 8u);
+    const int nb = (k + 3) / 4;
+    if (wide)
+        k_rl_index_nodes<u128><<<blocks, 256, 0, s>>>((const u128 *)nkey, part_off, node_base, noff, dense_base,
+                                                      part_nodes, n_buckets, nparts, nb, rpart, roff, rlen);
+    else
+        k_rl_index_nodes<uint64_t><<<blocks, 256, 0, s>>>((const uint64_t *)nkey, part_off, node_base, noff,
+                                                          dense_base, part_nodes, n_buckets, nparts, nb, rpart, roff,
+                                                          rlen);
+}
+
+template <class Src>
+static void rl_regroup(const uint8_t *sbytes, Src src, uint32_t n_tiles, uint32_t nparts, unsigned long long *cnt,
+                       void *scratch, uint8_t *dst, cudaStream_t s) {
+    const uint64_t ncnt = (uint64_t)nparts * n_tiles;
+    const unsigned blocks = std::min<uint32_t>(n_tiles, 152u * 16u);
+    t_launches += 2;
+    k_rl_tile_bytes<Src><<<blocks, 256, 0, s>>>(src, n_tiles, nparts, cnt);
+    exclusive_scan_u64(cnt, cnt, ncnt, cnt + ncnt, scratch, s);
+    cudaFuncSetAttribute(k_rl_move<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize, RL_SMEM);
+    k_rl_move<Src><<<blocks, 256, RL_SMEM, s>>>(sbytes, src, n_tiles, nparts, cnt, dst);
+}
+
+void launch_rl_regroup_arrays(const uint8_t *sbytes, const uint32_t *rpart, const uint32_t *rlen,
+                              const unsigned long long *roff, uint64_t n, uint32_t nparts, unsigned long long *cnt,
+                              void *scratch, uint8_t *dst, cudaStream_t s) {
+    if (!n) return;
+    RecArrays src{rpart, rlen, roff, n};
+    rl_regroup(sbytes, src, rl_tiles(n), nparts, cnt, scratch, dst, s);
+}
+
+void launch_rl_regroup_nodes(const uint8_t *sbytes, const void *nkey, int wide, int k, const uint32_t *noff,
+                             const unsigned long long *node_base, const unsigned long long *part_off,
+                             const uint32_t *part_nodes, uint32_t n_buckets, uint32_t nparts, unsigned long long *cnt,
+                             void *scratch, uint8_t *dst, cudaStream_t s) {
+    if (!n_buckets) return;
+    const int nb = (k + 3) / 4;
+    if (wide) {
+        RecNodes<u128> src{(const u128 *)nkey, noff, node_base, part_off, part_nodes, nb, nparts};
+        rl_regroup(sbytes, src, n_buckets, nparts, cnt, scratch, dst, s);
+    } else {
+        RecNodes<uint64_t> src{(const uint64_t *)nkey, noff, node_base, part_off, part_nodes, nb, nparts};
+        rl_regroup(sbytes, src, n_buckets, nparts, cnt, scratch, dst, s);
+    }
+}
+
+void launch_rl_part_starts(const unsigned long long *off, uint32_t n_tiles, uint32_t nparts, unsigned long long total,
+                           unsigned long long *bounds, cudaStream_t s) {
+    t_launches++;
+    k_rl_part_starts<<<(nparts + 256) / 256, 256, 0, s>>>(off, n_tiles, nparts, total, bounds);
+}
 
 void launch_rl_count(const uint32_t *key, const uint32_t *val, uint64_t n, int shift, uint32_t *cnt, cudaStream_t s) {
     const uint32_t t = rl_tiles(n);

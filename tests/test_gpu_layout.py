@@ -78,6 +78,19 @@ def test_more_parts_than_records(ctx):
     check_parts_vs_oracle(ctx, text, 5, 64)
 
 
+def test_giant_record_reference_layout(ctx):
+    """A node whose read heads make its record larger than one round's shared-memory stage."""
+    import random
+    rnd = random.Random(7)
+    head = "".join(rnd.choice("ACGT") for _ in range(25))
+    lines = []
+    for i in range(6000):
+        tail = "".join(rnd.choice("ACGT") for _ in range(75))
+        lines.append(f"{i}\t{head}{tail}")
+    text = ("\n".join(lines) + "\n").encode()
+    check_parts_vs_oracle(ctx, text, 21, 5)
+
+
 def test_empty_input_reference_layout(ctx):
     job = build(ctx, b"", 21, 4)
     assert job.part_offsets() == [0] * 5
