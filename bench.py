@@ -385,6 +385,30 @@ def bench_batched(ctx, samples, steps, warmup, local):
                                   "aggregate": got[0]["ms_aggregate"], "write": got[0]["ms_write"]}}
 
 
+def host_link(local, h2d_bytes, d2h_bytes, reps=3):
+    """The host link's copy rates, measured with plain copies of the e2e step's sizes between
+    pinned host memory and HBM (the best of `reps`)."""
+    import torch
+
+    dev = torch.empty(max(h2d_bytes, d2h_bytes), dtype=torch.uint8, device=f"cuda:{local}")
+    host = torch.empty(max(h2d_bytes, d2h_bytes), dtype=torch.uint8, pin_memory=True)
+    s = torch.cuda.current_stream()
+    out = {}
+    for name, n, dst, src in (("d2h_gbs", d2h_bytes, host, dev), ("h2d_gbs", h2d_bytes, dev, host)):
+        best = None
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            dst[:n].copy_(src[:n], non_blocking=True)
+            b.record(s)
+            b.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        out[name] = n / (best / 1e3) / 1e9
+    del dev, host
+    return out
+
+
 def bench_layout(ctx, w, d_text, warmup, pin, parts=LAYOUT_PARTS, reps=3):
     """The same build written into the reference's part layout (records regrouped by the
     reference's Kmer partitioner, one extra pass on the device): its cost beside the job's."""
@@ -513,6 +537,7 @@ def run_gb300(args, ws, rank, local):
     ctx.mark(3)
     ms_e2e = max_over_ranks(ws, ctx.elapsed_ms(2, 3))
     e2e_value = ws * args.steps * kmers / (ms_e2e / 1e3)
+    link = host_link(local, len(w.text), out_bytes)
 
     lay = None
     if not args.no_layout:
@@ -550,7 +575,11 @@ def run_gb300(args, ws, rank, local):
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": len(w.text),
                 "d2h_bytes_per_step": out_bytes, "ms_per_step": ms_e2e / args.steps,
-                "pipelined": "job i's record copy to the host overlaps job i+1's input copy and build"},
+                "pipelined": "job i's record copy to the host overlaps job i+1's input copy and build",
+                "host_link": link,
+                "link_bound_ms_per_step": (out_bytes / link["d2h_gbs"] + len(w.text) / link["h2d_gbs"]) / 1e6,
+                "link_bound_note": "both copies through the host link one after the other: the bound if "
+                                   "the link does not carry both directions at full rate at once"},
         "roofline": {"bound": "hbm", "kernel": "k_emit_write_part", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth",
                      "traffic": traffic, "alg_bytes_per_launch": wr_bytes, "ms_per_launch": wr_ms,
