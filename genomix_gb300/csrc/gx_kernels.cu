@@ -2502,6 +2502,27 @@ __device__ __forceinline__ uint32_t head_lower_bound(const HeadOut *hout, uint32
     return lo;
 }
 
+// The same search done by a warp: 32 evenly spaced heads narrow the range each round, so a
+// partition of up to 32 heads costs one round of loads instead of a chain of them.  All lanes
+// call it and get the same answer.
+__device__ __forceinline__ uint32_t warp_head_lower_bound(const HeadOut *hout, uint32_t hc, unsigned long long x,
+                                                          int lane) {
+    uint32_t lo = 0, hi = hc;
+    while (hi - lo > 32) {
+        const uint32_t step = (hi - lo + 31) / 32;
+        const uint32_t idx = lo + (uint32_t)lane * step;
+        const bool below = idx < hi && (unsigned long long)hout[idx].pos < x;
+        const uint32_t c = __popc(__ballot_sync(0xffffffffu, below));  // the samples below x lead
+        if (c == 0) return lo;
+        const uint32_t nlo = lo + (c - 1) * step + 1, nhi = min(hi, lo + c * step);
+        lo = nlo;
+        hi = nhi;
+    }
+    const uint32_t idx = lo + (uint32_t)lane;
+    const bool below = idx < hi && (unsigned long long)hout[idx].pos < x;
+    return lo + __popc(__ballot_sync(0xffffffffu, below));
+}
+
 // window [W, wend) of the partition out to global memory with aligned 16-byte stores
 __device__ __forceinline__ void window_out(uint8_t *out, const uint8_t *stage, unsigned long long g0,
                                            unsigned long long g1, int lane) {
@@ -2581,8 +2602,9 @@ __global__ void __launch_bounds__(WRITER_WARPS * 32, sizeof(K) == 8 ? 4 : 3) k_e
             ja++;
             continue;
         }
-        // ---- records [ja, jb): the most that fit in one window ----
+        // ---- records [ja, jb): the most that fit in one window (usually all the warp's) ----
         uint32_t lo = ja + 1, hi = j1;
+        if (off_at(j1) - W <= WARP_STAGE) lo = j1;
         while (lo < hi) {
             const uint32_t mid = (lo + hi + 1) >> 1;
             if (off_at(mid) - W <= WARP_STAGE)
@@ -2657,7 +2679,7 @@ __global__ void __launch_bounds__(WRITER_WARPS * 32, sizeof(K) == 8 ? 4 : 3) k_e
             carry = __shfl_sync(full, lv, 31);
         }
         __syncwarp();
-        const uint32_t hlo = head_lower_bound(hout, hc, W), hhi = head_lower_bound(hout, hc, wend);
+        const uint32_t hlo = warp_head_lower_bound(hout, hc, W, lane), hhi = warp_head_lower_bound(hout, hc, wend, lane);
         if (hlo < hhi) write_heads_window(Sink{stage, (long long)W, (long long)wend, false}, hout, hlo, hhi, a.text, lane);
         __syncwarp();
         window_out(a.out, stage, base + W, base + wend, lane);
