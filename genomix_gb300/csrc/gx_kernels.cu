@@ -2464,28 +2464,96 @@ __device__ __noinline__ void write_record_bytes(const Sink &o, long long st, lon
     o.u32(en - 4, cov);
 }
 
-// the read-head sets of heads [hlo, hhi) that touch the window
+__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
+    const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src), hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+// the letters of packed bytes j = lane and lane + 32 of an L-letter sequence (L <= 256), loaded
+// before any of them is used; missing letters read as 'A'
+__device__ __forceinline__ void load_seq_letters(const uint8_t *s, uint32_t L, int lane, uint32_t c[2][4]) {
+    const uint32_t nbr = packed_len(L);
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const uint32_t j = (uint32_t)lane + 32u * it;
+        const uint32_t i0 = 4 * (nbr - 1 - j);
+#pragma unroll
+        for (int q = 0; q < 4; q++) c[it][q] = (j < nbr && i0 + q < L) ? (uint32_t)s[i0 + q] : (uint32_t)'A';
+    }
+}
+
+__device__ __forceinline__ void store_seq_letters(const Sink &o, long long pos, uint32_t L, int lane,
+                                                  const uint32_t c[2][4]) {
+    const uint32_t nbr = packed_len(L);
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const uint32_t j = (uint32_t)lane + 32u * it;
+        if (j < nbr) {
+            uint32_t v = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) v |= base_code_checked(c[it][q]) << (2 * q);
+            o.b(pos + j, v);
+        }
+    }
+}
+
+// the read-head sets of heads [hlo, hhi) that touch the window.  Lane h loads head h's fields
+// (32 heads at a time); per head, each lane writes one header byte and two packed bytes of each
+// sequence, every letter of both sequences loaded before any byte is stored.  Sequences longer
+// than 256 letters take the byte-at-a-time path.
 __device__ __forceinline__ void write_heads_window(const Sink &ow, const HeadOut *hout, uint32_t hlo, uint32_t hhi,
                                                    const uint8_t *text, int lane) {
-    for (uint32_t h = hlo; h < hhi; h++) {
-        const HeadOut ho = hout[h];
-        const uint32_t nbr = packed_len(ho.L), nbm = packed_len(ho.Lm);
-        const long long hp = ho.pos;
-        const long long hsz = 13 + nbr + (ho.Lm ? 4 + nbm : 0);
-        if (!ow.touches(hp - (ho.set_count ? 5 : 0), hsz + 5)) continue;
-        if (lane == 0) {
-            if (ho.set_count) {
-                ow.b(hp - 5, 1);  // ExternalableTreeSet: whole body in stream
-                ow.u32(hp - 4, ho.set_count);
+    const unsigned full = 0xffffffffu;
+    for (uint32_t h0 = hlo; h0 < hhi; h0 += 32) {
+        const uint32_t nh = min(32u, hhi - h0);
+        HeadOut mine{};
+        if ((uint32_t)lane < nh) mine = hout[h0 + lane];
+        for (uint32_t q = 0; q < nh; q++) {
+            const uint32_t L = __shfl_sync(full, mine.L, q), Lm = __shfl_sync(full, mine.Lm, q);
+            const long long hp = (long long)__shfl_sync(full, mine.pos, q);
+            const uint32_t setc = __shfl_sync(full, mine.set_count, q);
+            const unsigned long long uuid = shfl64(mine.uuid, q);
+            const unsigned long long s_off = shfl64(mine.s_off, q), m_off = shfl64(mine.m_off, q);
+            const uint32_t nbr = packed_len(L), nbm = packed_len(Lm);
+            const long long hsz = 13 + nbr + (Lm ? 4 + nbm : 0);
+            if (!ow.touches(hp - (setc ? 5 : 0), hsz + 5)) continue;
+            // header bytes, one lane each: [set flag, set count], flags, uuid, L, and Lm after the read
+            bool put = false;
+            long long at = 0;
+            uint32_t v = 0;
+            if (lane < 5) {
+                put = setc != 0;  // ExternalableTreeSet: whole body in stream, then the count
+                at = hp - 5 + lane;
+                v = lane == 0 ? 1u : (setc >> (8 * (4 - lane))) & 0xffu;
+            } else if (lane == 5) {
+                put = true;
+                at = hp;
+                v = Lm ? 1u : 0u;
+            } else if (lane < 14) {
+                put = true;
+                at = hp + 1 + (lane - 6);
+                v = (uint32_t)(uuid >> (8 * (13 - lane))) & 0xffu;
+            } else if (lane < 18) {
+                put = true;
+                at = hp + 9 + (lane - 14);
+                v = (L >> (8 * (17 - lane))) & 0xffu;
+            } else if (lane < 22) {
+                put = Lm != 0;
+                at = hp + 13 + nbr + (lane - 18);
+                v = (Lm >> (8 * (21 - lane))) & 0xffu;
             }
-            ow.b(hp, ho.Lm ? 1u : 0u);
-            ow.u32(hp + 1, (uint32_t)(ho.uuid >> 32));
-            ow.u32(hp + 5, (uint32_t)ho.uuid);
-            ow.u32(hp + 9, ho.L);
-            if (ho.Lm) ow.u32(hp + 13 + nbr, ho.Lm);
+            if (put) ow.b(at, v);
+            if (nbr <= 64 && nbm <= 64) {
+                uint32_t cs[2][4], cm[2][4];
+                load_seq_letters(text + s_off, L, lane, cs);
+                load_seq_letters(text + m_off, Lm, lane, cm);
+                store_seq_letters(ow, hp + 13, L, lane, cs);
+                if (Lm) store_seq_letters(ow, hp + 17 + nbr, Lm, lane, cm);
+            } else {
+                pack_seq_warp(ow, hp + 13, text + s_off, L, lane);
+                if (Lm) pack_seq_warp(ow, hp + 17 + nbr, text + m_off, Lm, lane);
+            }
         }
-        pack_seq_warp(ow, hp + 13, text + ho.s_off, ho.L, lane);
-        if (ho.Lm) pack_seq_warp(ow, hp + 17 + nbr, text + ho.m_off, ho.Lm, lane);
     }
 }
 
