@@ -365,6 +365,7 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         a.node_base = fine_off;
         a.noff = noff;
         a.hout = hout;
+        a.n_head_slots = n_reads;
         CK(cudaEventRecord(tm.ev[5], s));
         launch_emit_write_part(a, s);
         CK(cudaEventRecord(tm.ev[6], s));

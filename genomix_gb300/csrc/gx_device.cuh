@@ -263,7 +263,9 @@ struct HeadOut {
     uint32_t pos;                     // partition-local byte position of the ReadHeadInfo
     uint32_t set_count;               // > 0 on the first head of a set: heads in the set
     uint32_t L, Lm;                   // read and mate lengths (Lm = 0: no mate sequence)
+    uint32_t part;                    // the partition (fine bucket); HEAD_DROPPED for a duplicate
 };
+constexpr uint32_t HEAD_DROPPED = 0xffffffffu;
 
 // ---- per-line parse output ---------------------------------------------------------------
 struct LineRec {

@@ -1010,6 +1010,7 @@ static gx_status build_partitioned(RunCtx &rc) {
         a.node_base = fine_off;
         a.noff = noff;
         a.hout = hout;
+        a.n_head_slots = n_reads;
         CK(cudaEventRecord(tm.ev[5], s));
         launch_emit_write_part(a, s);
         CK(cudaEventRecord(tm.ev[6], s));

@@ -2274,8 +2274,12 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
                 ho.Lm = mate ? lr.l0 : lr.l1;
                 ho.pos = sm.nbytes[rank] + 8 + keylen + 1 + edges + 5 + ((flipped && cu > 0) ? 5 : 0) + (pre - pre0);
                 ho.set_count = (wkept_idx == st && !flipped) ? cu : ((flipped && wkept_idx == st + cu) ? cf : 0u);
+                ho.part = f;
                 hout[wkept_idx] = ho;
             }
+            // the slots past the kept heads: duplicates, skipped by the head writer
+            const uint32_t kept_w = __popc(wkeep_mask);
+            if ((uint32_t)lane >= kept_w && (uint32_t)lane < hc) hout[lane].part = HEAD_DROPPED;
         }
     } else {
         unsigned long long hrun = 0;
@@ -2332,8 +2336,10 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
             ho.Lm = mate ? lr.l0 : lr.l1;
             ho.pos = pos;
             ho.set_count = (i == st && !flipped) ? cu : ((flipped && i == st + cu) ? cf : 0u);
+            ho.part = f;
             hout[i] = ho;
         }
+        for (uint32_t i = kept + threadIdx.x; i < hc; i += blockDim.x) hout[i].part = HEAD_DROPPED;
     }
     if (threadIdx.x == 0) {
         a.part_nodes[f] = n;
@@ -2497,98 +2503,65 @@ __device__ __forceinline__ void store_seq_letters(const Sink &o, long long pos, 
     }
 }
 
-// the read-head sets of heads [hlo, hhi) that touch the window.  Lane h loads head h's fields
-// (32 heads at a time); per head, each lane writes one header byte and two packed bytes of each
-// sequence, every letter of both sequences loaded before any byte is stored.  Sequences longer
-// than 256 letters take the byte-at-a-time path.
-__device__ __forceinline__ void write_heads_window(const Sink &ow, const HeadOut *hout, uint32_t hlo, uint32_t hhi,
-                                                   const uint8_t *text, int lane) {
-    const unsigned full = 0xffffffffu;
-    for (uint32_t h0 = hlo; h0 < hhi; h0 += 32) {
-        const uint32_t nh = min(32u, hhi - h0);
-        HeadOut mine{};
-        if ((uint32_t)lane < nh) mine = hout[h0 + lane];
-        for (uint32_t q = 0; q < nh; q++) {
-            const uint32_t L = __shfl_sync(full, mine.L, q), Lm = __shfl_sync(full, mine.Lm, q);
-            const long long hp = (long long)__shfl_sync(full, mine.pos, q);
-            const uint32_t setc = __shfl_sync(full, mine.set_count, q);
-            const unsigned long long uuid = shfl64(mine.uuid, q);
-            const unsigned long long s_off = shfl64(mine.s_off, q), m_off = shfl64(mine.m_off, q);
-            const uint32_t nbr = packed_len(L), nbm = packed_len(Lm);
-            const long long hsz = 13 + nbr + (Lm ? 4 + nbm : 0);
-            if (!ow.touches(hp - (setc ? 5 : 0), hsz + 5)) continue;
-            // header bytes, one lane each: [set flag, set count], flags, uuid, L, and Lm after the read
-            bool put = false;
-            long long at = 0;
-            uint32_t v = 0;
-            if (lane < 5) {
-                put = setc != 0;  // ExternalableTreeSet: whole body in stream, then the count
-                at = hp - 5 + lane;
-                v = lane == 0 ? 1u : (setc >> (8 * (4 - lane))) & 0xffu;
-            } else if (lane == 5) {
-                put = true;
-                at = hp;
-                v = Lm ? 1u : 0u;
-            } else if (lane < 14) {
-                put = true;
-                at = hp + 1 + (lane - 6);
-                v = (uint32_t)(uuid >> (8 * (13 - lane))) & 0xffu;
-            } else if (lane < 18) {
-                put = true;
-                at = hp + 9 + (lane - 14);
-                v = (L >> (8 * (17 - lane))) & 0xffu;
-            } else if (lane < 22) {
-                put = Lm != 0;
-                at = hp + 13 + nbr + (lane - 18);
-                v = (Lm >> (8 * (21 - lane))) & 0xffu;
-            }
-            if (put) ow.b(at, v);
-            if (nbr <= 64 && nbm <= 64) {
-                uint32_t cs[2][4], cm[2][4];
-                load_seq_letters(text + s_off, L, lane, cs);
-                load_seq_letters(text + m_off, Lm, lane, cm);
-                store_seq_letters(ow, hp + 13, L, lane, cs);
-                if (Lm) store_seq_letters(ow, hp + 17 + nbr, Lm, lane, cm);
-            } else {
-                pack_seq_warp(ow, hp + 13, text + s_off, L, lane);
-                if (Lm) pack_seq_warp(ow, hp + 17 + nbr, text + m_off, Lm, lane);
-            }
-        }
+// One read head and, on the first head of a set, the set's header: each lane writes one header
+// byte and two packed bytes of each sequence, every letter of both sequences loaded before any
+// byte is stored.  Sequences longer than 256 letters take the byte-at-a-time path.
+__device__ __forceinline__ void write_head(const Sink &ow, long long hp, uint32_t L, uint32_t Lm, uint32_t setc,
+                                           unsigned long long uuid, const uint8_t *s, const uint8_t *m, int lane) {
+    const uint32_t nbr = packed_len(L), nbm = packed_len(Lm);
+    // header bytes, one lane each: [set flag, set count], flags, uuid, L, and Lm after the read
+    bool put = false;
+    long long at = 0;
+    uint32_t v = 0;
+    if (lane < 5) {
+        put = setc != 0;  // ExternalableTreeSet: whole body in stream, then the count
+        at = hp - 5 + lane;
+        v = lane == 0 ? 1u : (setc >> (8 * (4 - lane))) & 0xffu;
+    } else if (lane == 5) {
+        put = true;
+        at = hp;
+        v = Lm ? 1u : 0u;
+    } else if (lane < 14) {
+        put = true;
+        at = hp + 1 + (lane - 6);
+        v = (uint32_t)(uuid >> (8 * (13 - lane))) & 0xffu;
+    } else if (lane < 18) {
+        put = true;
+        at = hp + 9 + (lane - 14);
+        v = (L >> (8 * (17 - lane))) & 0xffu;
+    } else if (lane < 22) {
+        put = Lm != 0;
+        at = hp + 13 + nbr + (lane - 18);
+        v = (Lm >> (8 * (21 - lane))) & 0xffu;
+    }
+    if (put) ow.b(at, v);
+    if (nbr <= 64 && nbm <= 64) {
+        uint32_t cs[2][4], cm[2][4];
+        load_seq_letters(s, L, lane, cs);
+        load_seq_letters(m, Lm, lane, cm);
+        store_seq_letters(ow, hp + 13, L, lane, cs);
+        if (Lm) store_seq_letters(ow, hp + 17 + nbr, Lm, lane, cm);
+    } else {
+        pack_seq_warp(ow, hp + 13, s, L, lane);
+        if (Lm) pack_seq_warp(ow, hp + 17 + nbr, m, Lm, lane);
     }
 }
 
-// first head at or after partition-local position x (heads are sorted by position)
-__device__ __forceinline__ uint32_t head_lower_bound(const HeadOut *hout, uint32_t hc, unsigned long long x) {
-    uint32_t lo = 0, hi = hc;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if ((unsigned long long)hout[mid].pos < x)
-            lo = mid + 1;
-        else
-            hi = mid;
+// The read-head sets of the partitioned build, straight into the record stream after the record
+// writer: the writer leaves those byte ranges to this kernel (it copies whatever its window held
+// there).  One warp per head slot; slots of dropped duplicates are skipped.
+__global__ void __launch_bounds__(256) k_write_heads_part(const HeadOut *hout, uint64_t n,
+                                                          const unsigned long long *part_off, const uint8_t *text,
+                                                          uint8_t *out) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const Sink o{out, 0, 0, true};
+    for (uint64_t h = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < n; h += nw) {
+        const HeadOut ho = hout[h];
+        if (ho.part == HEAD_DROPPED) continue;
+        write_head(o, (long long)(part_off[ho.part] + ho.pos), ho.L, ho.Lm, ho.set_count, ho.uuid, text + ho.s_off,
+                   text + ho.m_off, lane);
     }
-    return lo;
-}
-
-// The same search done by a warp: 32 evenly spaced heads narrow the range each round, so a
-// partition of up to 32 heads costs one round of loads instead of a chain of them.  All lanes
-// call it and get the same answer.
-__device__ __forceinline__ uint32_t warp_head_lower_bound(const HeadOut *hout, uint32_t hc, unsigned long long x,
-                                                          int lane) {
-    uint32_t lo = 0, hi = hc;
-    while (hi - lo > 32) {
-        const uint32_t step = (hi - lo + 31) / 32;
-        const uint32_t idx = lo + (uint32_t)lane * step;
-        const bool below = idx < hi && (unsigned long long)hout[idx].pos < x;
-        const uint32_t c = __popc(__ballot_sync(0xffffffffu, below));  // the samples below x lead
-        if (c == 0) return lo;
-        const uint32_t nlo = lo + (c - 1) * step + 1, nhi = min(hi, lo + c * step);
-        lo = nlo;
-        hi = nhi;
-    }
-    const uint32_t idx = lo + (uint32_t)lane;
-    const bool below = idx < hi && (unsigned long long)hout[idx].pos < x;
-    return lo + __popc(__ballot_sync(0xffffffffu, below));
 }
 
 // window [W, wend) of the partition out to global memory with aligned 16-byte stores
@@ -2628,12 +2601,10 @@ __global__ void __launch_bounds__(WRITER_WARPS * 32, sizeof(K) == 8 ? 4 : 3) k_e
     const uint32_t n = a.part_nodes[p];
     const unsigned long long pbytes = a.part_bytes[p];
     const unsigned long long base = a.part_off[p];
-    const uint32_t hb = a.head_off[p], hc = a.head_cnt2[p];
     const unsigned long long nbase = a.node_base[p];
     const K *nkey = (const K *)a.nkey + nbase;
     const unsigned long long *ncm = a.ncm + nbase;
     const uint32_t *noff = a.noff + nbase;
-    const HeadOut *hout = a.hout + hb;
     const uint32_t npw = (n + WRITER_WARPS - 1) / WRITER_WARPS;
     const uint32_t j0 = min(n, warp * npw), j1 = min(n, j0 + npw);
     // record j starts at off_at(j); off_at(n) is the partition's end
@@ -2656,13 +2627,10 @@ __global__ void __launch_bounds__(WRITER_WARPS * 32, sizeof(K) == 8 ? 4 : 3) k_e
             if (meta & META_FLIPPED) active |= 0x20u;
             const uint32_t cov = __float_as_uint((float)(uint32_t)cm);
             const K key = nkey[ja];
-            const uint32_t hlo = head_lower_bound(hout, hc, W), hhi = head_lower_bound(hout, hc, en);
             for (unsigned long long Wg = W; Wg < en; Wg += WARP_STAGE) {
                 const unsigned long long we = min(en, Wg + WARP_STAGE);
                 const Sink o{stage, (long long)Wg, (long long)we, false};
                 if (lane == 0) write_record_bytes<K>(o, (long long)W, (long long)en, key, meta, active, cov, k, nb);
-                __syncwarp();
-                write_heads_window(o, hout, hlo, hhi, a.text, lane);
                 __syncwarp();
                 window_out(a.out, stage, base + Wg, base + we, lane);
                 __syncwarp();
@@ -2747,9 +2715,6 @@ __global__ void __launch_bounds__(WRITER_WARPS * 32, sizeof(K) == 8 ? 4 : 3) k_e
             carry = __shfl_sync(full, lv, 31);
         }
         __syncwarp();
-        const uint32_t hlo = warp_head_lower_bound(hout, hc, W, lane), hhi = warp_head_lower_bound(hout, hc, wend, lane);
-        if (hlo < hhi) write_heads_window(Sink{stage, (long long)W, (long long)wend, false}, hout, hlo, hhi, a.text, lane);
-        __syncwarp();
         window_out(a.out, stage, base + W, base + wend, lane);
         __syncwarp();
         ja = jb;
@@ -2766,6 +2731,11 @@ void launch_emit_write_part(const EmitArgs &a, cudaStream_t s) {
     } else {
         cudaFuncSetAttribute(k_emit_write_part<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_emit_write_part<uint64_t><<<a.g.nparts, WRITER_WARPS * 32, sm, s>>>(a);
+    }
+    if (a.n_head_slots) {
+        t_launches++;
+        const unsigned blocks = (unsigned)std::min<uint64_t>((a.n_head_slots + 7) / 8, 152ull * 64);
+        k_write_heads_part<<<blocks, 256, 0, s>>>(a.hout, a.n_head_slots, a.part_off, a.text, a.out);
     }
 }
 

@@ -86,6 +86,7 @@ struct EmitArgs {
     const unsigned long long *node_base = nullptr;
     const uint32_t *noff = nullptr;
     const HeadOut *hout = nullptr;
+    uint64_t n_head_slots = 0;   // entries of hout: kept heads and dropped duplicates
 };
 void launch_emit_prepare(const EmitArgs &a, cudaStream_t s);
 void launch_emit_write(const EmitArgs &a, cudaStream_t s);
