@@ -2549,18 +2549,29 @@ __device__ __forceinline__ void write_head(const Sink &ow, long long hp, uint32_
 
 // The read-head sets of the partitioned build, straight into the record stream after the record
 // writer: the writer leaves those byte ranges to this kernel (it copies whatever its window held
-// there).  One warp per head slot; slots of dropped duplicates are skipped.
+// there).  A warp takes 32 head slots at a time: lane h loads slot h and its partition's offset,
+// then the warp writes the heads one after another; slots of dropped duplicates are skipped.
 __global__ void __launch_bounds__(256) k_write_heads_part(const HeadOut *hout, uint64_t n,
                                                           const unsigned long long *part_off, const uint8_t *text,
                                                           uint8_t *out) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const Sink o{out, 0, 0, true};
-    for (uint64_t h = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < n; h += nw) {
-        const HeadOut ho = hout[h];
-        if (ho.part == HEAD_DROPPED) continue;
-        write_head(o, (long long)(part_off[ho.part] + ho.pos), ho.L, ho.Lm, ho.set_count, ho.uuid, text + ho.s_off,
-                   text + ho.m_off, lane);
+    for (uint64_t h0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; h0 < n; h0 += nw * 32) {
+        const uint32_t nh = n - h0 < 32 ? (uint32_t)(n - h0) : 32u;
+        HeadOut mine{};
+        mine.part = HEAD_DROPPED;
+        if ((uint32_t)lane < nh) mine = hout[h0 + lane];
+        const unsigned long long hp = mine.part != HEAD_DROPPED ? part_off[mine.part] + mine.pos : 0ull;
+        uint32_t live = __ballot_sync(full, mine.part != HEAD_DROPPED);
+        while (live) {
+            const int q = __ffs(live) - 1;
+            live &= live - 1;
+            write_head(o, (long long)shfl64(hp, q), __shfl_sync(full, mine.L, q), __shfl_sync(full, mine.Lm, q),
+                       __shfl_sync(full, mine.set_count, q), shfl64(mine.uuid, q), text + shfl64(mine.s_off, q),
+                       text + shfl64(mine.m_off, q), lane);
+        }
     }
 }
 
@@ -2734,7 +2745,7 @@ void launch_emit_write_part(const EmitArgs &a, cudaStream_t s) {
     }
     if (a.n_head_slots) {
         t_launches++;
-        const unsigned blocks = (unsigned)std::min<uint64_t>((a.n_head_slots + 7) / 8, 152ull * 64);
+        const unsigned blocks = (unsigned)std::min<uint64_t>((a.n_head_slots + 255) / 256, 152ull * 8);
         k_write_heads_part<<<blocks, 256, 0, s>>>(a.hout, a.n_head_slots, a.part_off, a.text, a.out);
     }
 }
