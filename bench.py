@@ -65,9 +65,9 @@ def peaks():
 
 
 def profiled_traffic(alg_bytes):
-    """DRAM bytes per record-writer launch from the committed ncu summary: the capture runs a
-    smaller case of the same workload, whose DRAM bytes per algorithmic byte scale to this
-    launch (the writer's traffic grows in proportion to the records it writes)."""
+    """DRAM bytes of one record-writer pass (the record writer and the read-head writer) from the
+    committed ncu summary: the capture runs a smaller case of the same workload, whose DRAM bytes
+    per algorithmic byte scale to this pass (the traffic grows in proportion to the records)."""
     if not os.path.exists(PROFILE_TRAFFIC):
         return None
     ratio = None
@@ -580,7 +580,8 @@ def run_gb300(args, ws, rank, local):
                 "link_bound_ms_per_step": (out_bytes / link["d2h_gbs"] + len(w.text) / link["h2d_gbs"]) / 1e6,
                 "link_bound_note": "both copies through the host link one after the other: the bound if "
                                    "the link does not carry both directions at full rate at once"},
-        "roofline": {"bound": "hbm", "kernel": "k_emit_write_part", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "k_emit_write_part + k_write_heads_part", "achieved": achieved,
+                     "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth",
                      "traffic": traffic, "alg_bytes_per_launch": wr_bytes, "ms_per_launch": wr_ms,
                      "unit_of_work": "record byte written (plus its node and read-head inputs)"},
