@@ -52,6 +52,8 @@ REF_STEP_PAIRS = 60_000      # --impl reference: sample per step
 TUNE_PAIRS = 200_000         # autotuner sample: the first pairs of the workload
 LAYOUT_PARTS = 16            # parts of the reference part layout measurement
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_emit_write_part_pe5mbp_k31.md")
+PROFILE_TRAFFIC_AGG = os.path.join(ROOT, "profiles", "k_aggregate_pe5mbp_k31.md")
+AGG_HEAD_BYTES = 112         # per read head in k_aggregate: Head read and written, HeadOut, its read's line
 HEADOUT_BYTES = 48           # one HeadOut entry (uuid, two text offsets, position, counts)
 
 
@@ -64,18 +66,26 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(alg_bytes):
+def profiled_traffic(alg_bytes, path=PROFILE_TRAFFIC):
     """DRAM bytes of one record-writer pass (the record writer and the read-head writer) from the
     committed ncu summary: the capture runs a smaller case of the same workload, whose DRAM bytes
     per algorithmic byte scale to this pass (the traffic grows in proportion to the records)."""
-    if not os.path.exists(PROFILE_TRAFFIC):
+    if not os.path.exists(path):
         return None
     ratio = None
-    with open(PROFILE_TRAFFIC) as f:
+    with open(path) as f:
         for line in f:
             if line.startswith("dram_bytes_per_algorithmic_byte:"):
                 ratio = float(line.split(":")[1])
     return None if ratio is None else ratio * alg_bytes
+
+
+def aggregate_alg_bytes(st, k):
+    """Bytes k_aggregate must move per launch: every occurrence's key and edge bits read once,
+    each node's key, count/meta word and record offset written once, and per read head its
+    Head entry (read and updated), its HeadOut entry and its read's line record."""
+    kb = 8 if k <= 32 else 16
+    return st["kmers"] * (kb + 2) + st["nodes"] * (kb + 12) + st["read_heads"] * AGG_HEAD_BYTES
 
 
 def writer_alg_bytes(st, k, read_len, paired):
@@ -561,6 +571,9 @@ def run_gb300(args, ws, rank, local):
     wr_bytes = writer_alg_bytes(stats[0], w.k, 150, True)
     achieved = wr_bytes / (wr_ms / 1e3) / 1e9
     traffic = profiled_traffic(wr_bytes)
+    agg_ms = statistics.mean(s["ms_aggregate"] for s in stats)
+    agg_bytes = aggregate_alg_bytes(stats[0], w.k)
+    agg_achieved = agg_bytes / (agg_ms / 1e3) / 1e9
     b_alg = len(w.text) + 64.0 * kmers + out_bytes
     job_ms = ms / args.steps
     cb = None
@@ -580,17 +593,23 @@ def run_gb300(args, ws, rank, local):
                 "link_bound_ms_per_step": (out_bytes / link["d2h_gbs"] + len(w.text) / link["h2d_gbs"]) / 1e6,
                 "link_bound_note": "both copies through the host link one after the other: the bound if "
                                    "the link does not carry both directions at full rate at once"},
-        "roofline": {"bound": "hbm", "kernel": "k_emit_write_part + k_write_heads_part", "achieved": achieved,
-                     "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth",
-                     "traffic": traffic, "alg_bytes_per_launch": wr_bytes, "ms_per_launch": wr_ms,
-                     "unit_of_work": "record byte written (plus its node and read-head inputs)"},
+        "roofline": {"bound": "hbm", "kernel": "k_aggregate", "achieved": agg_achieved, "peak": peak,
+                     "unit": "GB/s", "frac": agg_achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth",
+                     "traffic": profiled_traffic(agg_bytes, PROFILE_TRAFFIC_AGG), "alg_bytes_per_launch": agg_bytes,
+                     "ms_per_launch": agg_ms,
+                     "unit_of_work": "k-mer occurrence aggregated (10 B read; 20 B per node and 112 B per read "
+                                     "head written)"},
+        "roofline_writer": {"bound": "hbm", "kernel": "k_emit_write_part + k_write_heads_part", "achieved": achieved,
+                            "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                            "peak_kind": f"{peak_kind} copy bandwidth", "traffic": traffic,
+                            "alg_bytes_per_launch": wr_bytes, "ms_per_launch": wr_ms,
+                            "unit_of_work": "record byte written (plus its node and read-head inputs)"},
         "random_access": {"bound_kmers_per_s": peak * 1e9 / 64.0, "frac": value / ws / (peak * 1e9 / 64.0),
                           "note": "64 B per k-mer occurrence (one 32 B sector read + one written)"},
         "job_roofline": {"alg_bytes": b_alg, "achieved_gbs": b_alg / (job_ms / 1e3) / 1e9,
                          "frac": b_alg / (job_ms / 1e3) / 1e9 / peak},
         "phases_ms": {"parse": statistics.mean(s["ms_parse"] for s in stats), "partition": ins_ms,
-                      "aggregate": statistics.mean(s["ms_aggregate"] for s in stats), "write": wr_ms,
+                      "aggregate": agg_ms, "write": wr_ms,
                       "job": job_ms},
         "graph": {"kmers": kmers, "reads": stats[0]["reads"], "nodes": stats[0]["nodes"],
                   "read_heads": stats[0]["read_heads"], "record_bytes": out_bytes,
