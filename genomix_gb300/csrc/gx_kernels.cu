@@ -2475,32 +2475,17 @@ __device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int s
     return ((unsigned long long)hi << 32) | lo;
 }
 
-// the letters of packed bytes j = lane and lane + 32 of an L-letter sequence (L <= 256), loaded
-// before any of them is used; missing letters read as 'A'
-__device__ __forceinline__ void load_seq_letters(const uint8_t *s, uint32_t L, int lane, uint32_t c[2][4]) {
-    const uint32_t nbr = packed_len(L);
-#pragma unroll
-    for (int it = 0; it < 2; it++) {
-        const uint32_t j = (uint32_t)lane + 32u * it;
-        const uint32_t i0 = 4 * (nbr - 1 - j);
-#pragma unroll
-        for (int q = 0; q < 4; q++) c[it][q] = (j < nbr && i0 + q < L) ? (uint32_t)s[i0 + q] : (uint32_t)'A';
-    }
-}
-
-__device__ __forceinline__ void store_seq_letters(const Sink &o, long long pos, uint32_t L, int lane,
-                                                  const uint32_t c[2][4]) {
-    const uint32_t nbr = packed_len(L);
-#pragma unroll
-    for (int it = 0; it < 2; it++) {
-        const uint32_t j = (uint32_t)lane + 32u * it;
-        if (j < nbr) {
-            uint32_t v = 0;
-#pragma unroll
-            for (int q = 0; q < 4; q++) v |= base_code_checked(c[it][q]) << (2 * q);
-            o.b(pos + j, v);
-        }
-    }
+// Four letters (the first in the low byte) packed into one VKmer byte, first letter in the low
+// bits: A/a=0 C/c=1 G/g=2 T/t=3, any other byte 0 (GeneCode.getCodeFromSymbol), four at a time.
+__device__ __forceinline__ uint32_t pack4_letters(uint32_t w) {
+    const uint32_t u = w & 0xDFDFDFDFu;
+    const uint32_t ok = zero_bytes(u ^ 0x41414141u) | zero_bytes(u ^ 0x43434343u) | zero_bytes(u ^ 0x47474747u) |
+                        zero_bytes(u ^ 0x54545454u);
+    uint32_t c = (w >> 1) & 0x03030303u;  // A 0, C 1, G 3, T 2 in each byte
+    c ^= (c >> 1) & 0x01010101u;          // G 2, T 3
+    c &= (ok >> 7) * 3u;                  // other bytes 0
+    const uint32_t y = c | (c >> 6);
+    return (y | (y >> 12)) & 0xFFu;
 }
 
 // One read head and, on the first head of a set, the set's header: each lane writes one header
@@ -2535,15 +2520,31 @@ __device__ __forceinline__ void write_head(const Sink &ow, long long hp, uint32_
         v = (Lm >> (8 * (21 - lane))) & 0xffu;
     }
     if (put) ow.b(at, v);
-    if (nbr <= 64 && nbm <= 64) {
-        uint32_t cs[2][4], cm[2][4];
-        load_seq_letters(s, L, lane, cs);
-        load_seq_letters(m, Lm, lane, cm);
-        store_seq_letters(ow, hp + 13, L, lane, cs);
-        if (Lm) store_seq_letters(ow, hp + 17 + nbr, Lm, lane, cm);
-    } else {
-        pack_seq_warp(ow, hp + 13, s, L, lane);
-        if (Lm) pack_seq_warp(ow, hp + 17 + nbr, m, Lm, lane);
+    // the packed bytes of both sequences as one run of nbr + nbm, 128 at a time: byte t < nbr is
+    // read byte t, the rest mate bytes; byte j of a sequence holds letters 4 (nb - 1 - j) + 0..3
+    const uint32_t tot = nbr + nbm;
+    for (uint32_t t0 = 0; t0 < tot; t0 += 128) {
+        uint32_t w[4];
+#pragma unroll
+        for (int it = 0; it < 4; it++) {
+            const uint32_t t = t0 + (uint32_t)lane + 32u * it;
+            const bool mate = t >= nbr;
+            const uint8_t *q = mate ? m : s;
+            const uint32_t len = mate ? Lm : L, j = mate ? t - nbr : t;
+            const uint32_t i0 = 4 * ((mate ? nbm : nbr) - 1 - j);
+            uint32_t x = 0;
+            if (t < tot) {
+#pragma unroll
+                for (int c = 0; c < 4; c++)
+                    if (i0 + c < len) x |= (uint32_t)q[i0 + c] << (8 * c);
+            }
+            w[it] = x;
+        }
+#pragma unroll
+        for (int it = 0; it < 4; it++) {
+            const uint32_t t = t0 + (uint32_t)lane + 32u * it;
+            if (t < tot) ow.b(t < nbr ? hp + 13 + t : hp + 17 + t, pack4_letters(w[it]));
+        }
     }
 }
 
