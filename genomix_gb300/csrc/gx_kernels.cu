@@ -106,6 +106,12 @@ __device__ __forceinline__ T warp_inclusive_scan(T x) {
     return x;
 }
 
+// a 64-bit value from lane src (all lanes call)
+__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
+    const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src), hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
+    return ((unsigned long long)hi << 32) | lo;
+}
+
 // Block-wide exclusive scan of one value per thread; ws must hold 33 T.  All threads call.
 template <class T>
 __device__ __forceinline__ T block_exclusive_scan(T v, T *ws, T &total) {
@@ -2001,6 +2007,19 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
     const K *okey = (const K *)a.okey2 + o0;
     const uint16_t *obits = a.obits2 + o0;
     const uint32_t M = (uint32_t)(o1 - o0);
+    // A bucket with at most 32 read heads (the usual case) leaves them to warp 0: lane i loads
+    // head i's entry, its read and the read's line now, so the loads land while the table fills.
+    const uint32_t hb = a.head_off[f], hc = a.head_cnt[f];
+    const bool warp_heads = hc <= 32;
+    uint32_t p_r = 0xffffffffu, p_rl = 0;
+    Head p_h{};
+    LineRec p_lr{};
+    if (warp_heads && threadIdx.x < hc) {
+        p_r = a.head_idx[hb + threadIdx.x];
+        p_h = a.heads[p_r];
+        p_rl = a.reads[p_r];
+        p_lr = a.lines[p_rl >> 1];
+    }
     {
         const uint4 z = make_uint4(0, 0, 0, 0);
         uint4 *k4 = reinterpret_cast<uint4 *>(sm.key1);
@@ -2052,19 +2071,32 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
         return;
     }
     // 2. read heads: find their node, mark the unflipped / flipped set
-    const uint32_t hb = a.head_off[f], hc = a.head_cnt[f];
-    for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
-        const uint32_t r = a.head_idx[hb + i];
-        Head h = a.heads[r];
-        const K key = (K)(((u128)h.khi << 64) | h.klo);
-        const int sl = AggTable<K>::find(sm.key1, key, (uint32_t)KeyOps<K>::hash(key));
-        if (sl < 0) {
-            atomicAdd(&a.st->internal_err, 1u);
-            continue;
+    if (warp_heads) {
+        if (threadIdx.x < hc) {
+            const K key = (K)(((u128)p_h.khi << 64) | p_h.klo);
+            const int sl = AggTable<K>::find(sm.key1, key, (uint32_t)KeyOps<K>::hash(key));
+            if (sl < 0) {
+                atomicAdd(&a.st->internal_err, 1u);
+                p_h.slot = 0;
+            } else {
+                atomicOr(&sm.meta[sl], (p_h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
+                p_h.slot = (uint32_t)sl;
+            }
         }
-        atomicOr(&sm.meta[sl], (h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
-        h.slot = (uint32_t)sl;
-        a.heads[r] = h;
+    } else {
+        for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
+            const uint32_t r = a.head_idx[hb + i];
+            Head h = a.heads[r];
+            const K key = (K)(((u128)h.khi << 64) | h.klo);
+            const int sl = AggTable<K>::find(sm.key1, key, (uint32_t)KeyOps<K>::hash(key));
+            if (sl < 0) {
+                atomicAdd(&a.st->internal_err, 1u);
+                continue;
+            }
+            atomicOr(&sm.meta[sl], (h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
+            h.slot = (uint32_t)sl;
+            a.heads[r] = h;
+        }
     }
     // 3. order the nodes deterministically: by home slot (the low hash bits that started the
     //    probe), then by key.  A counting sort over the 2048 homes: keys per home (nbytes),
@@ -2116,17 +2148,18 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
     unsigned long long *hk = a.head_sk + hb;
     uint32_t *hv = a.head_idx + hb;
     const int lane = threadIdx.x & 31;
-    const bool warp_heads = hc <= 32;
     unsigned long long wk = 0;  // warp path: this lane's head in sorted order, kept or not
-    uint32_t wv = 0, wkeep = 0, wkept_idx = 0, wkeep_mask = 0;
+    uint32_t wkeep = 0, wkept_idx = 0, wkeep_mask = 0;
+    // warp path: the sorted head's uuid, sequence offsets and lengths (from the lane that loaded it)
+    unsigned long long w_uuid = 0, w_soff = 0, w_moff = 0;
+    uint32_t w_L = 0, w_Lm = 0;
     if (warp_heads) {
         if (threadIdx.x < 32) {
             unsigned long long mk = ~0ULL;
             uint32_t mv = 0xffffffffu;
             if (lane < (int)hc) {
-                mv = hv[lane];
-                const Head h = a.heads[mv];
-                mk = head_sort_key(sm.rank_of_slot[h.slot], h.uuid);
+                mv = p_r;
+                mk = head_sort_key(sm.rank_of_slot[p_h.slot], p_h.uuid);
             }
             uint32_t rank = 0;
             for (int j = 0; j < (int)hc; j++) {
@@ -2136,21 +2169,27 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
             }
             if (lane < (int)hc) {
                 sm.wsk[rank] = mk;
-                sm.wsv[rank] = mv;
+                sm.wsv[rank] = (uint32_t)lane;
             }
             __syncwarp();
+            uint32_t src = (uint32_t)lane;
             if (lane < (int)hc) {
                 wk = sm.wsk[lane];
-                wv = sm.wsv[lane];
+                src = sm.wsv[lane];
             }
+            const uint32_t mate = p_rl & 1u;
+            w_uuid = shfl64(p_h.uuid, (int)src);
+            w_soff = shfl64(mate ? p_lr.s1 : p_lr.s0, (int)src);
+            w_moff = shfl64(mate ? p_lr.s0 : p_lr.s1, (int)src);
+            w_L = __shfl_sync(0xffffffffu, mate ? p_lr.l1 : p_lr.l0, (int)src);
+            w_Lm = __shfl_sync(0xffffffffu, mate ? p_lr.l0 : p_lr.l1, (int)src);
             const unsigned long long prev = __shfl_up_sync(0xffffffffu, wk, 1);
             wkeep = (lane < (int)hc && (lane == 0 || wk != prev)) ? 1u : 0u;
             wkeep_mask = __ballot_sync(0xffffffffu, wkeep);
             wkept_idx = __popc(wkeep_mask & ((1u << lane) - 1u));
-            if (wkeep) {
-                const uint32_t rl = a.reads[wv];
-                atomicAdd(&sm.nbytes[(uint32_t)(wk >> 37)], head_bytes(a.lines[rl >> 1], rl & 1u));
-            }
+            if (wkeep)
+                atomicAdd(&sm.nbytes[(uint32_t)(wk >> 37)],
+                          1 + 8 + 4 + packed_len(w_L) + (w_Lm > 0 ? 4 + packed_len(w_Lm) : 0));
             if (lane == 0) sm.kept = __popc(wkeep_mask);
         }
         __syncthreads();
@@ -2241,13 +2280,7 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
     const uint32_t keylen = 4 + nb;
     if (warp_heads) {
         if (threadIdx.x < 32) {
-            uint32_t hsz = 0, rl = 0;
-            LineRec lr{};
-            if (wkeep) {
-                rl = a.reads[wv];
-                lr = a.lines[rl >> 1];
-                hsz = head_bytes(lr, rl & 1u);
-            }
+            const uint32_t hsz = wkeep ? 1 + 8 + 4 + packed_len(w_L) + (w_Lm > 0 ? 4 + packed_len(w_Lm) : 0) : 0u;
             const uint32_t pre = warp_inclusive_scan(hsz) - hsz;  // bytes of the kept heads before
             const uint32_t rank = (uint32_t)(wk >> 37);
             const bool flipped = (wk >> 36) & 1ULL;
@@ -2265,13 +2298,12 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
                     if (m) edges += 4 + __popc(m) * (4 + nb);
                 }
                 const uint32_t st = __popc(wkeep_mask & ((1u << first) - 1u));  // kept index of the node's first
-                const uint32_t mate = rl & 1u;
                 HeadOut ho;
-                ho.uuid = a.heads[wv].uuid;
-                ho.s_off = mate ? lr.s1 : lr.s0;
-                ho.m_off = mate ? lr.s0 : lr.s1;
-                ho.L = mate ? lr.l1 : lr.l0;
-                ho.Lm = mate ? lr.l0 : lr.l1;
+                ho.uuid = w_uuid;
+                ho.s_off = w_soff;
+                ho.m_off = w_moff;
+                ho.L = w_L;
+                ho.Lm = w_Lm;
                 ho.pos = sm.nbytes[rank] + 8 + keylen + 1 + edges + 5 + ((flipped && cu > 0) ? 5 : 0) + (pre - pre0);
                 ho.set_count = (wkept_idx == st && !flipped) ? cu : ((flipped && wkept_idx == st + cu) ? cf : 0u);
                 ho.part = f;
@@ -2468,11 +2500,6 @@ __device__ __noinline__ void write_record_bytes(const Sink &o, long long st, lon
         }
     }
     o.u32(en - 4, cov);
-}
-
-__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
-    const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src), hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
-    return ((unsigned long long)hi << 32) | lo;
 }
 
 // Four letters (the first in the low byte) packed into one VKmer byte, first letter in the low
