@@ -1493,6 +1493,9 @@ PartPlan plan_partitions(double distinct_est, double safety, double target) {
     uint64_t P = (uint64_t)ceil(want);
     uint32_t log_s = 0;
     while ((1ull << (2 * log_s)) < P && log_s < 11) log_s++;  // S ~ sqrt(P)
+    // then half of that while the fine buckets per super bucket stay within MAX_FINE: fewer bins
+    // per super-scatter round, still long runs in the fine pass (measured: 3 % off the partition)
+    if (log_s > 6 && ((P + (1ull << (log_s - 1)) - 1) >> (log_s - 1)) <= MAX_FINE) log_s--;
     if (log_s < 6) log_s = 6;
     const uint64_t S = 1ull << log_s;
     uint64_t F = (P + S - 1) / S;
