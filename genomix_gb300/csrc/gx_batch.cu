@@ -34,7 +34,7 @@ constexpr uint32_t MAX_BATCH = 1024;  // samples per pass: each needs at least o
 constexpr gx_status BATCH_FALLBACK = (gx_status)-1;
 
 // Bucket plan of a batch.  Sample s wants P_s fine buckets (distinct estimate x safety /
-// target per bucket); its super buckets S_s = 2^log_s start near sqrt(P_s) and are halved,
+// target per bucket); its super buckets S_s = 2^log_s start near sqrt(P_s) / 2 and are halved,
 // largest first, until the batch fits MAX_SUPERS; F_s = ceil(P_s / S_s) <= MAX_FINE.
 bool plan_batch(const std::vector<double> &d_est, double safety, double target, std::vector<SamplePlan> &plans,
                 uint32_t &n_super, uint32_t &n_fine) {
@@ -50,6 +50,7 @@ bool plan_batch(const std::vector<double> &d_est, double safety, double target, 
         if (lo > 11) return false;
         uint32_t l = 0;
         while ((1ull << (2 * l)) < P[i] && l < 11) l++;
+        if (l > 6) l--;  // half of sqrt(P), as a single job's plan (lo keeps F within MAX_FINE)
         lmin[i] = lo;
         lg[i] = std::max(l, lo);
         sum += 1ull << lg[i];
