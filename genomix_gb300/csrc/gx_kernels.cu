@@ -1341,6 +1341,10 @@ struct Walker {
         xo = s_off;
         xn = 0;
         xbuf = 0;
+        // the read's sectors requested up front: the walk then consumes them from L1 instead of
+        // waiting on one 8-byte load after another
+        for (unsigned long long a = s_off & ~31ULL; a < s_off + L && a < n_text; a += 32)
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(text + a));
         k = k_;
         sh = 2 * (k - 1);
         mask = KeyOps<K>::mask(k);
