@@ -287,7 +287,8 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         CK(cudaMemsetAsync(head_cur, 0, P * 4ull, s));
         const SampleMap smap{read_base, d_plan, n};
         CK(cudaEventRecord(tm.ev[2], s));
-        launch_scatter_super(wide, text, n_text, lines, reads, n_reads, k, smap, S, d_soff, s_cur, okey, obits, s);
+        launch_scatter_super(wide, text, n_text, lines, reads, n_reads, k, smap, S, d_soff, s_cur, okey, obits,
+                             0xffffffffu, nullptr, nullptr, s);
         launch_heads_part(wide, text, n_text, lines, reads, n_reads, k, smap, heads, head_cnt, s);
         exclusive_scan_u32(head_cnt, head_off, P, nullptr, pscratch, s);
         launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, P, s);

@@ -454,7 +454,7 @@ struct RunCtx {
     uint32_t *reads;
     uint32_t n_lines, n_reads;
     unsigned long long n_occ;
-    // partitioned build: A1 results (2048 super counts, HyperLogLog registers)
+    // partitioned build: exact super counts (2048) and HyperLogLog registers, when it counted
     uint32_t *d_scnt, *d_hll;
     std::vector<uint32_t> scnt, hll;
 };
@@ -825,7 +825,35 @@ static gx_status build_read_parser(RunCtx &rc) {
     return GX_OK;
 }
 
-// ---- the partitioned build --------------------------------------------------------------
+// the exact super counts and HyperLogLog registers of the whole input (a counting pass)
+static gx_status count_supers(RunCtx &rc) {
+    cudaStream_t s = rc.s;
+    gx_status e;
+    if (!rc.d_scnt) {
+        if ((e = rc.ar.alloc(rc.d_scnt, MAX_SUPERS)) != GX_OK) return e;
+        if ((e = rc.ar.alloc(rc.d_hll, HLL_REGS)) != GX_OK) return e;
+    }
+    CK(cudaMemsetAsync(rc.d_scnt, 0, MAX_SUPERS * 4, s));
+    CK(cudaMemsetAsync(rc.d_hll, 0, HLL_REGS * 4, s));
+    uint32_t *d_n;
+    if ((e = rc.ar.alloc(d_n, 1)) != GX_OK) return e;
+    CK(cudaMemcpyAsync(d_n, &rc.n_reads, 4, cudaMemcpyHostToDevice, s));
+    launch_count_occ(rc.j->wide, rc.text, rc.n_text, rc.lines, rc.reads, d_n, rc.n_reads, rc.j->k, 11, rc.d_scnt,
+                     rc.d_hll, s);
+    rc.scnt.resize(MAX_SUPERS);
+    rc.hll.resize(HLL_REGS);
+    CK(d2h_async(rc.scnt.data(), rc.d_scnt, MAX_SUPERS * 4, s));
+    CK(d2h_async(rc.hll.data(), rc.d_hll, HLL_REGS * 4, s));
+    CK(sync_stream(s));
+    CK(cudaGetLastError());
+    return GX_OK;
+}
+
+// ---- the partitioned build ---------------------------------------------------------------
+// A job's first pass needs no counting pass: the super scatter writes into buckets with room
+// for SC_ROOM x the mean (the hash spreads k-mers evenly; only a k-mer repeated very many times
+// can fill one) and gathers the HyperLogLog registers on the way, which size the fine buckets.
+// If a bucket runs out of room, the job counts its super buckets exactly and scatters again.
 static gx_status build_partitioned(RunCtx &rc) {
     gx_job *j = rc.j;
     cudaStream_t s = rc.s;
@@ -835,30 +863,22 @@ static gx_status build_partitioned(RunCtx &rc) {
     const uint32_t n_reads = rc.n_reads;
     const uint64_t n_occ = rc.n_occ;
     const size_t kb = wide ? 16 : 8;
-    const double d_est = hll_estimate(rc.hll.data());
     double safety = 1.15;
     DevStatus hs;
+    bool counted = !rc.scnt.empty();
+    if (!counted && n_occ / 2 > 0xfffffff0ULL - SC_SLACK) {  // bucket cursors are 32-bit
+        if ((e = count_supers(rc)) != GX_OK) return e;
+        counted = true;
+    }
+    double d_est = counted ? hll_estimate(rc.hll.data()) : 0.0;
     for (int attempt = 0;; attempt++) {
         const double target = bucket_target(j->eff_load_factor);
-        const PartPlan pp = plan_partitions(d_est, safety, target);
-        const uint32_t S = 1u << pp.log_s, P = pp.P;
-        // super counts at this resolution, offsets and CHUNK-sized pieces
-        std::vector<unsigned long long> soff(S + 1, 0);
-        const uint32_t fold = MAX_SUPERS >> pp.log_s;
-        for (uint32_t q = 0; q < S; q++) {
-            unsigned long long c = 0;
-            for (uint32_t t = 0; t < fold; t++) c += rc.scnt[q * fold + t];
-            soff[q + 1] = soff[q] + c;
-        }
-        if (soff[S] != n_occ) return GX_ECUDA;
-        std::vector<ulonglong2> chunks;
-        chunks.reserve(n_occ / CHUNK + S + 1);
-        for (uint32_t q = 0; q < S; q++)
-            for (unsigned long long st = soff[q]; st < soff[q + 1]; st += CHUNK) {
-                const unsigned long long len = std::min<unsigned long long>(CHUNK, soff[q + 1] - st);
-                chunks.push_back(make_ulonglong2(st, ((unsigned long long)q << 32) | len));
-            }
-        const uint32_t n_chunks = (uint32_t)chunks.size();
+        // super buckets: from the distinct estimate, or (before any count) from the occurrences,
+        // which bound the distinct k-mers
+        PartPlan pp = plan_partitions(counted ? d_est : (double)n_occ, safety, target);
+        const uint32_t S = 1u << pp.log_s;
+        const uint64_t cap = counted ? 0 : std::min<uint64_t>(0xfffffff0ULL, (uint64_t)((double)n_occ / S * SC_ROOM) + SC_SLACK);
+        const uint64_t occ_room = counted ? n_occ : std::max<uint64_t>(n_occ, (uint64_t)S * cap);
         RunArena tar(s);
         void *okey, *okey2;
         uint16_t *obits, *obits2;
@@ -869,31 +889,19 @@ static gx_status build_partitioned(RunCtx &rc) {
         HeadOut *hout;
         uint32_t *noff;
         uint8_t *okey_b, *okey2_b;
-        if ((e = tar.alloc(okey_b, n_occ * kb)) != GX_OK) return e;
+        if ((e = tar.alloc(okey_b, occ_room * kb)) != GX_OK) return e;
         if ((e = tar.alloc(okey2_b, n_occ * kb)) != GX_OK) return e;
         okey = okey_b;
         okey2 = okey2_b;
-        if ((e = tar.alloc(obits, n_occ)) != GX_OK) return e;
+        if ((e = tar.alloc(obits, occ_room)) != GX_OK) return e;
         if ((e = tar.alloc(obits2, n_occ)) != GX_OK) return e;
         if ((e = tar.alloc(d_soff, S + 1)) != GX_OK) return e;
-        if ((e = tar.alloc(d_chunks, std::max<uint32_t>(n_chunks, 1))) != GX_OK) return e;
         if ((e = tar.alloc(s_cur, S)) != GX_OK) return e;
-        if ((e = tar.alloc(fine_cnt, P)) != GX_OK) return e;
-        if ((e = tar.alloc(fine_off, P + 1)) != GX_OK) return e;
-        if ((e = tar.alloc(fine_cur, P)) != GX_OK) return e;
         if ((e = tar.alloc(heads, n_reads)) != GX_OK) return e;
         if ((e = tar.alloc(hout, n_reads)) != GX_OK) return e;
         if ((e = tar.alloc(noff, n_occ)) != GX_OK) return e;
-        if ((e = tar.alloc(head_cnt, P)) != GX_OK) return e;
-        if ((e = tar.alloc(head_off, P)) != GX_OK) return e;
-        if ((e = tar.alloc(head_cur, P)) != GX_OK) return e;
         if ((e = tar.alloc(head_idx, n_reads)) != GX_OK) return e;
-        if ((e = tar.alloc(head_cnt2, P)) != GX_OK) return e;
         if ((e = tar.alloc(head_sk, n_reads)) != GX_OK) return e;
-        if ((e = tar.alloc(part_nodes, P)) != GX_OK) return e;
-        if ((e = tar.alloc(part_bytes, P)) != GX_OK) return e;
-        void *pscratch;
-        if ((e = tar.alloc(pscratch, scan_scratch_bytes(P + 1, 8))) != GX_OK) return e;
         // the job is a batch of one sample
         SamplePlan *d_plan;
         SuperInfo *d_sinfo;
@@ -901,31 +909,110 @@ static gx_status build_partitioned(RunCtx &rc) {
         if ((e = tar.alloc(d_plan, 1)) != GX_OK) return e;
         if ((e = tar.alloc(d_sinfo, S)) != GX_OK) return e;
         if ((e = tar.alloc(d_rbase, 2)) != GX_OK) return e;
+        const SampleMap smap{d_rbase, d_plan, 1};
+        {
+            const uint32_t hrb[2] = {0, n_reads};
+            CK(cudaMemcpyAsync(d_rbase, hrb, sizeof hrb, cudaMemcpyHostToDevice, s));
+        }
+        std::vector<unsigned long long> soff(S + 1, 0);
+        std::vector<uint32_t> scount(S, 0);
+        CK(cudaMemsetAsync(s_cur, 0, S * 4ull, s));
+        CK(cudaEventRecord(tm.ev[2], s));
+        if (!counted) {
+            // A2 first, with room per bucket; the HyperLogLog registers come back with the counts
+            uint32_t *d_hll, *d_ovf;
+            if ((e = tar.alloc(d_hll, SC_HLL_REGS)) != GX_OK) return e;
+            if ((e = tar.alloc(d_ovf, 1)) != GX_OK) return e;
+            CK(cudaMemsetAsync(d_hll, 0, SC_HLL_REGS * 4, s));
+            CK(cudaMemsetAsync(d_ovf, 0, 4, s));
+            for (uint32_t q = 0; q <= S; q++) soff[q] = (unsigned long long)q * cap;
+            const SamplePlan hp{0, pp.log_s, 1, 0};
+            CK(cudaMemcpyAsync(d_plan, &hp, sizeof hp, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(d_soff, soff.data(), (S + 1) * 8ull, cudaMemcpyHostToDevice, s));
+            launch_scatter_super(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, S, d_soff, s_cur,
+                                 okey, obits, (uint32_t)cap, d_hll, d_ovf, s);
+            std::vector<uint32_t> hh(SC_HLL_REGS);
+            uint32_t ovf = 0;
+            CK(d2h_async(scount.data(), s_cur, S * 4ull, s));
+            CK(d2h_async(hh.data(), d_hll, SC_HLL_REGS * 4, s));
+            CK(d2h_async(&ovf, d_ovf, 4, s));
+            CK(sync_stream(s));
+            CK(cudaGetLastError());
+            if (ovf) {
+                // a bucket needed more room: count exactly, then scatter again (not an attempt)
+                tar.release();
+                if ((e = count_supers(rc)) != GX_OK) return e;
+                counted = true;
+                d_est = hll_estimate(rc.hll.data());
+                attempt--;
+                continue;
+            }
+            if (attempt == 0) d_est = hll_estimate(hh.data(), SC_HLL_REGS);
+            // fine buckets for this S
+            double want = d_est * safety / target;
+            const uint64_t P64 = (uint64_t)std::max(1.0, std::ceil(want));
+            pp.F = (uint32_t)std::min<uint64_t>(MAX_FINE, std::max<uint64_t>(1, (P64 + S - 1) / S));
+            pp.P = S * pp.F;
+        } else {
+            // super counts at this resolution, offsets
+            const uint32_t fold = MAX_SUPERS >> pp.log_s;
+            for (uint32_t q = 0; q < S; q++) {
+                unsigned long long c = 0;
+                for (uint32_t t = 0; t < fold; t++) c += rc.scnt[q * fold + t];
+                scount[q] = (uint32_t)c;
+                soff[q + 1] = soff[q] + c;
+            }
+            if (soff[S] != n_occ) return GX_ECUDA;
+        }
+        const uint32_t P = pp.P;
+        // CHUNK-sized pieces of every super bucket
+        std::vector<ulonglong2> chunks;
+        chunks.reserve(n_occ / CHUNK + S + 1);
+        uint64_t placed = 0;
+        for (uint32_t q = 0; q < S; q++) {
+            placed += scount[q];
+            for (unsigned long long st = 0; st < scount[q]; st += CHUNK) {
+                const unsigned long long len = std::min<unsigned long long>(CHUNK, scount[q] - st);
+                chunks.push_back(make_ulonglong2(soff[q] + st, ((unsigned long long)q << 32) | len));
+            }
+        }
+        if (placed != n_occ) return GX_ECUDA;
+        const uint32_t n_chunks = (uint32_t)chunks.size();
+        if ((e = tar.alloc(d_chunks, std::max<uint32_t>(n_chunks, 1))) != GX_OK) return e;
+        if ((e = tar.alloc(fine_cnt, P)) != GX_OK) return e;
+        if ((e = tar.alloc(fine_off, P + 1)) != GX_OK) return e;
+        if ((e = tar.alloc(fine_cur, P)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cnt, P)) != GX_OK) return e;
+        if ((e = tar.alloc(head_off, P)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cur, P)) != GX_OK) return e;
+        if ((e = tar.alloc(head_cnt2, P)) != GX_OK) return e;
+        if ((e = tar.alloc(part_nodes, P)) != GX_OK) return e;
+        if ((e = tar.alloc(part_bytes, P)) != GX_OK) return e;
+        void *pscratch;
+        if ((e = tar.alloc(pscratch, scan_scratch_bytes(P + 1, 8))) != GX_OK) return e;
         {
             const SamplePlan hp{0, pp.log_s, pp.F, 0};
             std::vector<SuperInfo> hsi(S);
             for (uint32_t q = 0; q < S; q++) hsi[q] = SuperInfo{q * pp.F, pp.F, pp.log_s, 0};
-            const uint32_t hrb[2] = {0, n_reads};
             CK(cudaMemcpyAsync(d_plan, &hp, sizeof hp, cudaMemcpyHostToDevice, s));
             CK(cudaMemcpyAsync(d_sinfo, hsi.data(), S * sizeof(SuperInfo), cudaMemcpyHostToDevice, s));
-            CK(cudaMemcpyAsync(d_rbase, hrb, sizeof hrb, cudaMemcpyHostToDevice, s));
         }
-        const SampleMap smap{d_rbase, d_plan, 1};
         void *part_off_v = nullptr;
         CK(cudaMallocAsync(&part_off_v, (P + 1) * sizeof(unsigned long long), s));
         part_off = (unsigned long long *)part_off_v;
-        CK(cudaMemcpyAsync(d_soff, soff.data(), (S + 1) * 8ull, cudaMemcpyHostToDevice, s));
         if (n_chunks)
             CK(cudaMemcpyAsync(d_chunks, chunks.data(), n_chunks * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
-        CK(cudaMemsetAsync(s_cur, 0, S * 4ull, s));
         CK(cudaMemsetAsync(fine_cnt, 0, P * 8ull, s));
         CK(cudaMemsetAsync(fine_cur, 0, P * 4ull, s));
         CK(cudaMemsetAsync(head_cnt, 0, P * 4ull, s));
         CK(cudaMemsetAsync(head_cur, 0, P * 4ull, s));
-        CK(cudaEventRecord(tm.ev[2], s));
-        // A2, read heads
-        launch_scatter_super(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, S, d_soff, s_cur, okey,
-                             obits, s);
+        if (counted) {
+            // A2 into the counted offsets
+            CK(cudaMemcpyAsync(d_soff, soff.data(), (S + 1) * 8ull, cudaMemcpyHostToDevice, s));
+            launch_scatter_super(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, S, d_soff, s_cur,
+                                 okey, obits, 0xffffffffu, nullptr, nullptr, s);
+        }
+        // read heads
         launch_heads_part(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, heads, head_cnt, s);
         exclusive_scan_u32(head_cnt, head_off, P, nullptr, pscratch, s);
         launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, P, s);
@@ -1170,12 +1257,6 @@ static gx_status run_job(gx_job *j) {
     if ((e = ar.alloc(tile_cnt, tiles + 1)) != GX_OK) return e;
     if ((e = ar.alloc(d_nlines, 4)) != GX_OK) return e;
     if ((e = ar.alloc(scratch, scratch_bytes)) != GX_OK) return e;
-    if (partitioned) {
-        if ((e = ar.alloc(d_scnt, MAX_SUPERS)) != GX_OK) return e;
-        if ((e = ar.alloc(d_hll, HLL_REGS)) != GX_OK) return e;
-        CK(cudaMemsetAsync(d_scnt, 0, MAX_SUPERS * 4, s));
-        CK(cudaMemsetAsync(d_hll, 0, HLL_REGS * 4, s));
-    }
 
     // ---- K1 ----
     CK(cudaEventRecord(tm.ev[0], s));
@@ -1198,21 +1279,12 @@ static gx_status run_job(gx_job *j) {
     launch_parse_lines(text, n_text, line_end, n_lines, k, lines, lflags, nvalid, d_st, s);
     exclusive_scan_u32(nvalid, nvalid, n_lines, d_nlines + 1, scratch, s);
     launch_read_list(lflags, nvalid, lines, n_lines, k, reads, d_st, s);
-    // A1 of the partitioned build runs before the host learns the read count
-    if (partitioned)
-        launch_count_occ(j->wide, text, n_text, lines, reads, d_nlines + 1, 2 * n_lines, k, 11, d_scnt, d_hll, s);
     CK(cudaEventRecord(tm.ev[1], s));
     DevStatus hs;
     uint32_t n_reads = 0;
     RunCtx rc{j, s, ar, d_st, scratch, text, n_text, lines, reads, n_lines, 0, 0, d_scnt, d_hll, {}, {}};
     CK(d2h_async(&hs, d_st, sizeof hs, s));
     CK(d2h_async(&n_reads, d_nlines + 1, 4, s));
-    if (partitioned) {
-        rc.scnt.resize(MAX_SUPERS);
-        rc.hll.resize(HLL_REGS);
-        CK(d2h_async(rc.scnt.data(), d_scnt, MAX_SUPERS * 4, s));
-        CK(d2h_async(rc.hll.data(), d_hll, HLL_REGS * 4, s));
-    }
     CK(sync_stream(s));
     CK(cudaGetLastError());
     if (hs.parse_err != ~0ULL) {

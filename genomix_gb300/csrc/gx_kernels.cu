@@ -1477,11 +1477,11 @@ __global__ void __launch_bounds__(256) k_count_occ(const uint8_t *text, unsigned
 }
 
 // HyperLogLog (Flajolet, Fusy, Gandouet, Meunier 2007) with the small-range correction
-double hll_estimate(const uint32_t *regs) {
-    const double m = HLL_REGS;
+double hll_estimate(const uint32_t *regs, int n_regs) {
+    const double m = n_regs;
     double z = 0;
     int zeros = 0;
-    for (int i = 0; i < HLL_REGS; i++) {
+    for (int i = 0; i < n_regs; i++) {
         z += ldexp(1.0, -(int)regs[i]);
         if (regs[i] == 0) zeros++;
     }
@@ -1625,6 +1625,7 @@ struct SuperSmem {
     uint16_t sup[SC_THREADS * SC_ROUND];
     uint32_t ws[33];
     uint32_t rounds, total;
+    uint32_t hll[SC_HLL_REGS];  // this block's HyperLogLog registers (when the build asks for them)
     uint32_t arrays[1];  // loff[S], gbase[S], cur[S]
     static size_t bytes(uint32_t S) { return sizeof(SuperSmem) + 3ull * S * sizeof(uint32_t); }
 };
@@ -1642,7 +1643,8 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
                                                               const uint32_t *reads, uint32_t n_reads, int k,
                                                               SampleMap m, uint32_t S,
                                                               const unsigned long long *s_off,
-                                                              uint32_t *s_cur, K *okey, uint16_t *obits) {
+                                                              uint32_t *s_cur, K *okey, uint16_t *obits,
+                                                              uint32_t cap, uint32_t *hll, uint32_t *ovf) {
     constexpr bool CACHE = SuperRound<K>::CACHE;
     constexpr int RN = SuperRound<K>::N;
     extern __shared__ __align__(16) uint8_t smem_raw[];
@@ -1660,6 +1662,8 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
         w.empty();
     }
     if (threadIdx.x == 0) sm.rounds = 0;
+    if (hll)
+        for (uint32_t i = threadIdx.x; i < SC_HLL_REGS; i += blockDim.x) sm.hll[i] = 0;
     __syncthreads();
     atomicMax(&sm.rounds, (w.nk + RN - 1) / RN);
     __syncthreads();
@@ -1678,8 +1682,14 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
             K c;
             uint32_t b, d;
             w.next(c, b, d);
-            const uint32_t sp = sbase + super_local(KeyOps<K>::hash(c), log_s);
+            const uint64_t h = KeyOps<K>::hash(c);
+            const uint32_t sp = sbase + super_local(h, log_s);
             atomicAdd(&sm_cur[sp], 1u);
+            if (hll) {
+                const uint64_t w2 = h >> 9;  // HyperLogLog: register = low 9 bits, rank of the rest
+                const uint32_t rho = w2 ? (uint32_t)(__clzll(w2) - 8) : 56u;
+                atomicMax(&sm.hll[h & (SC_HLL_REGS - 1)], rho);
+            }
             if (CACHE) {
                 ck[q] = c;
                 cb[q] = b | (sp << 16);
@@ -1687,8 +1697,14 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
         }
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) {
-            sm_loff[i] = sm_cur[i];
-            sm_gbase[i] = sm_cur[i] ? atomicAdd(&s_cur[i], sm_cur[i]) : 0u;
+            const uint32_t c = sm_cur[i];
+            sm_loff[i] = c;
+            uint32_t g = c ? atomicAdd(&s_cur[i], c) : 0u;
+            if (c && (unsigned long long)g + c > cap) {  // the bucket's room is used up: nothing of it is written
+                atomicOr(ovf, 1u);
+                g = 0xffffffffu;
+            }
+            sm_gbase[i] = g;
         }
         __syncthreads();
         const uint32_t tot = block_scan_array(sm_loff, S, sm.ws);
@@ -1719,18 +1735,22 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
         // write the runs out
         for (uint32_t i = threadIdx.x; i < tot; i += blockDim.x) {
             const uint32_t sp = sm.sup[i];
+            if (sm_gbase[sp] == 0xffffffffu) continue;
             const unsigned long long g = s_off[sp] + sm_gbase[sp] + (i - sm_loff[sp]);
             okey[g] = sm.key[i];
             obits[g] = sm.bits[i];
         }
         __syncthreads();
     }
+    if (hll)
+        for (uint32_t i = threadIdx.x; i < SC_HLL_REGS; i += blockDim.x)
+            if (sm.hll[i]) atomicMax(&hll[i], sm.hll[i]);
 }
 
 void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
                           const uint32_t *reads, uint32_t n_reads, int k, SampleMap m, uint32_t n_super,
                           const unsigned long long *s_off, uint32_t *s_cur, void *okey, uint16_t *obits,
-                          cudaStream_t s) {
+                          uint32_t cap, uint32_t *hll, uint32_t *ovf, cudaStream_t s) {
     if (!n_reads) return;
     const unsigned blocks = (n_reads + SC_THREADS - 1) / SC_THREADS;
     t_launches++;
@@ -1738,12 +1758,13 @@ void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const 
         const size_t sm = SuperSmem<u128>::bytes(n_super);
         cudaFuncSetAttribute(k_scatter_super<u128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_scatter_super<u128><<<blocks, SC_THREADS, sm, s>>>(text, n_text, lines, reads, n_reads, k, m, n_super,
-                                                             s_off, s_cur, (u128 *)okey, obits);
+                                                             s_off, s_cur, (u128 *)okey, obits, cap, hll, ovf);
     } else {
         const size_t sm = SuperSmem<uint64_t>::bytes(n_super);
         cudaFuncSetAttribute(k_scatter_super<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_scatter_super<uint64_t><<<blocks, SC_THREADS, sm, s>>>(text, n_text, lines, reads, n_reads, k, m,
-                                                                 n_super, s_off, s_cur, (uint64_t *)okey, obits);
+                                                                 n_super, s_off, s_cur, (uint64_t *)okey, obits, cap,
+                                                                 hll, ovf);
     }
 }
 

@@ -100,6 +100,11 @@ constexpr uint32_t AGG_TARGET = 896;         // distinct k-mers per fine bucket 
 constexpr uint32_t CHUNK = 4096;             // occurrences per CTA in the fine passes
 constexpr int SC_THREADS = 256;              // super scatter: one read per thread
 constexpr int SC_ROUND = 16;                 // k-mers per thread per staging round
+constexpr int SC_HLL_REGS = 512;             // HyperLogLog registers kept by the super scatter
+// A super scatter without a counting pass first: every super bucket gets room for this share of
+// the mean bucket plus SC_SLACK; a bucket that needs more sets the overflow flag.
+constexpr double SC_ROOM = 1.3;
+constexpr uint32_t SC_SLACK = 8192;
 constexpr uint32_t MAX_SUPERS = 2048, MAX_FINE = 2048;
 
 struct PartPlan {
@@ -108,7 +113,7 @@ struct PartPlan {
     uint32_t P;      // S * F
 };
 // distinct k-mer estimate from the HyperLogLog registers
-double hll_estimate(const uint32_t *regs);
+double hll_estimate(const uint32_t *regs, int n_regs = HLL_REGS);
 PartPlan plan_partitions(double distinct_est, double safety, double target);
 
 // Bucket plan of one sample.  A batch of samples shares one bucket space: sample s owns the
@@ -150,7 +155,7 @@ void launch_sample_bounds(const unsigned long long *text_base, uint32_t n_sample
 void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
                           const uint32_t *reads, uint32_t n_reads, int k, SampleMap m, uint32_t n_super,
                           const unsigned long long *s_off, uint32_t *s_cur, void *okey, uint16_t *obits,
-                          cudaStream_t s);
+                          uint32_t cap, uint32_t *hll, uint32_t *ovf, cudaStream_t s);
 // chunks: (start, super << 32 | length) of CHUNK-sized pieces of each super bucket
 void launch_fine_count(int wide, const void *okey, const ulonglong2 *chunks, uint32_t n_chunks,
                        const SuperInfo *sinfo, unsigned long long *fine_cnt, cudaStream_t s);
