@@ -39,6 +39,7 @@ import json
 import os
 import statistics
 import subprocess
+import threading
 import sys
 import time
 
@@ -109,13 +110,24 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        self.lines = []
+        self.first = threading.Event()
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (FileNotFoundError, OSError):
             self.proc = None
-        time.sleep(0.3)
+        if self.proc:
+            def reader():
+                for line in self.proc.stdout:
+                    self.lines.append(line)
+                    self.first.set()
+            self.thread = threading.Thread(target=reader, daemon=True)
+            self.thread.start()
+            # nvidia-smi's start-up talks to the driver: let it finish before the timed region
+            self.first.wait(timeout=10)
+            time.sleep(0.25)
         return self
 
     def __exit__(self, *a):
@@ -124,9 +136,11 @@ class ClockSampler:
             time.sleep(0.25)
             self.proc.terminate()
             try:
-                self.out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+            self.thread.join(timeout=5)
+            self.out = "".join(self.lines)
 
     def summary(self):
         sm, mx, reasons = [], None, set()
@@ -632,7 +646,7 @@ def run_gb300(args, ws, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
