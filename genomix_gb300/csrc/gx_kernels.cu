@@ -2026,7 +2026,7 @@ __device__ __forceinline__ uint32_t kept_lower_bound(const unsigned long long *h
 }
 
 template <class K>
-__global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
+__global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggArgs a) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     AggSmem<K> &sm = *reinterpret_cast<AggSmem<K> *>(smem_raw);
     const uint32_t f = blockIdx.x;
@@ -2048,6 +2048,17 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
         p_rl = a.reads[p_r];
         p_lr = a.lines[p_rl >> 1];
     }
+    // 1. aggregate the bucket's occurrences: count += 1, edge mask |= bits; each thread
+    //    loads AGG_BATCH occurrences before inserting any of them (the first batch's loads go
+    //    out before the table is cleared)
+    K kk[AGG_BATCH];
+    uint32_t bb[AGG_BATCH];
+#pragma unroll
+    for (int q = 0; q < AGG_BATCH; q++) {
+        const uint32_t i = q * blockDim.x + threadIdx.x;
+        kk[q] = i < M ? okey[i] : (K)0;
+        bb[q] = i < M ? (uint32_t)obits[i] : 0u;
+    }
     {
         const uint4 z = make_uint4(0, 0, 0, 0);
         uint4 *k4 = reinterpret_cast<uint4 *>(sm.key1);
@@ -2063,16 +2074,14 @@ __global__ void __launch_bounds__(256) k_aggregate(AggArgs a) {
         sm.fail = 0;
     }
     __syncthreads();
-    // 1. aggregate the bucket's occurrences: count += 1, edge mask |= bits; each thread
-    //    loads AGG_BATCH occurrences before inserting any of them
     for (uint32_t c0 = 0; c0 < M; c0 += AGG_BATCH * blockDim.x) {
-        K kk[AGG_BATCH];
-        uint32_t bb[AGG_BATCH];
+        if (c0) {
 #pragma unroll
-        for (int q = 0; q < AGG_BATCH; q++) {
-            const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
-            kk[q] = i < M ? okey[i] : (K)0;
-            bb[q] = i < M ? (uint32_t)obits[i] : 0u;
+            for (int q = 0; q < AGG_BATCH; q++) {
+                const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
+                kk[q] = i < M ? okey[i] : (K)0;
+                bb[q] = i < M ? (uint32_t)obits[i] : 0u;
+            }
         }
 #pragma unroll
         for (int q = 0; q < AGG_BATCH; q++) {
