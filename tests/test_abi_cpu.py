@@ -97,3 +97,66 @@ def test_records_digest_is_order_independent_and_counts():
     bad[first_len - 1] ^= 1
     d2 = gx.records_digest(bytes(bad))
     assert (d2["sum"], d2["xor_"]) != (d["sum"], d["xor_"])
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors have the C structs' sizes and field offsets (a C program compiled
+    against include/gxgpu.h prints them)."""
+    import ctypes
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {
+        "gx_job_opts": _lib.JobOpts, "gx_stats": _lib.Stats, "gx_serve_opts": _lib.ServeOpts,
+        "gx_serve_stats": _lib.ServeStats, "gx_digest": _lib.Digest, "gx_graph_stats": _lib.GraphStats,
+        "gx_ctx_opts": _lib.CtxOpts, "gx_stat_hist": _lib.StatHist, "gx_tune_result": _lib.TuneResult,
+    }
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "gxgpu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'    printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def java_part(kmer_bytes, nparts):
+    """KmerPartitionComputerFactory.hashBytes + partition (KmerPartitionComputerFactory.java:28-52),
+    in Python integers: h = 1, then 31 h + (signed) byte, as a Java int; sign-folded; mod parts."""
+    h = 1
+    for b in kmer_bytes:
+        h = (31 * h + (b - 256 if b > 127 else b)) & 0xFFFFFFFF
+    if h >= 1 << 31:
+        h -= 1 << 32
+    if h < 0:
+        h = -(h + 1)
+    return h % nparts
+
+
+@pytest.mark.parametrize("parts", [3, 7, 300])
+def test_oracle_parts_follow_the_reference_partitioner(parts):
+    """Every record of the oracle's part q has a key the restated partitioner sends to q: the
+    oracle's part layout, which the GPU's reference part layout is checked against, is pinned to
+    the reference's hash."""
+    from genomix_gb300 import synth
+    text = synth.plain_cpu().text
+    ref = go.build_graph(text, 21, threads=4, parts=parts)
+    assert ref.status == 0
+    po = ref.part_offsets
+    seen = 0
+    for q in range(parts):
+        for key, _ in gx.iter_records(ref.records[po[q]:po[q + 1]]):
+            assert java_part(key[4:], parts) == q
+            seen += 1
+    assert seen == ref.nodes
