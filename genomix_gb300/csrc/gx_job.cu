@@ -606,21 +606,38 @@ static gx_status relayout_reference_parts(RunCtx &rc, uint32_t &nparts, unsigned
     return GX_OK;
 }
 
+// After the record writer: its status (into hs), the node and head counts per partition and the
+// output parts' bounds, all read back in one round trip.
 static gx_status finish_outputs(RunCtx &rc, uint32_t nparts, unsigned long long total, unsigned long long *part_off,
-                                const uint32_t *part_nodes, const uint32_t *head_cnt2, void *outp,
+                                const uint32_t *part_nodes, const uint32_t *head_cnt2, void *outp, DevStatus &hs,
                                 const NodeRecords *nr = nullptr) {
     gx_job *j = rc.j;
     const int P = j->o.out_parts;
+    const bool regroup = j->o.layout == GX_LAYOUT_REFERENCE_PARTS && P > 1;
     std::vector<uint32_t> pn(nparts), hc(nparts);
+    std::vector<unsigned long long> bounds(P + 1, 0);
+    CK(d2h_async(&hs, rc.d_st, sizeof hs, rc.s));
     CK(d2h_async(pn.data(), part_nodes, nparts * 4ull, rc.s));
     CK(d2h_async(hc.data(), head_cnt2, nparts * 4ull, rc.s));
+    if (!regroup)
+        for (int q = 1; q < P; q++) {
+            const uint64_t tp = (uint64_t)nparts * q / P;
+            if (tp > 0) CK(d2h_async(&bounds[q], part_off + tp, 8, rc.s));
+        }
     CK(sync_stream(rc.s));
+    CK(cudaGetLastError());
+    if (hs.internal_err) {
+        cudaFreeAsync(outp, rc.s);
+        cudaFreeAsync(part_off, rc.s);
+        fprintf(stderr, "gxgpu: internal error: record sizes disagree between emission passes\n");
+        return GX_ECUDA;
+    }
     uint64_t nn = 0, nh = 0;
     for (uint32_t q = 0; q < nparts; q++) {
         nn += pn[q];
         nh += hc[q];
     }
-    if (j->o.layout == GX_LAYOUT_REFERENCE_PARTS && P > 1 && nn > 0) {
+    if (regroup && nn > 0) {
         const gx_status e = relayout_reference_parts(rc, nparts, total, pn, part_nodes, nn, nr, part_off, outp);
         if (e != GX_OK) {
             cudaFreeAsync(outp, rc.s);
@@ -628,16 +645,8 @@ static gx_status finish_outputs(RunCtx &rc, uint32_t nparts, unsigned long long 
             return e;
         }
     } else {
-        for (int q = 0; q <= P; q++) {
-            const uint64_t tp = (uint64_t)nparts * q / P;
-            unsigned long long v = 0;
-            if (q == P)
-                v = total;
-            else if (tp > 0)
-                CK(d2h_async(&v, part_off + tp, 8, rc.s));
-            CK(sync_stream(rc.s));
-            j->part_bounds[q] = v;
-        }
+        bounds[P] = total;
+        for (int q = 0; q <= P; q++) j->part_bounds[q] = bounds[q];
     }
     for (int q = 0; q < P; q++) j->cursor[q] = j->part_bounds[q];
     j->st.nodes = nn;
@@ -742,16 +751,7 @@ static gx_status build_table(RunCtx &rc) {
         CK(cudaEventRecord(tm.ev[5], s));
         launch_emit_write(a, s);
         CK(cudaEventRecord(tm.ev[6], s));
-        CK(d2h_async(&hs, rc.d_st, sizeof hs, s));
-        CK(sync_stream(s));
-        CK(cudaGetLastError());
-        if (hs.internal_err) {
-            cudaFreeAsync(outp, s);
-            cudaFreeAsync(part_off, s);
-            fprintf(stderr, "gxgpu: internal error: record sizes disagree between emission passes\n");
-            return GX_ECUDA;
-        }
-        if ((e = finish_outputs(rc, nparts, total, part_off, part_nodes, head_cnt2, outp)) != GX_OK) return e;
+        if ((e = finish_outputs(rc, nparts, total, part_off, part_nodes, head_cnt2, outp, hs)) != GX_OK) return e;
         j->st.table_slots = (uint64_t)nparts * PART_SLOTS;
         j->st.table_partitions = nparts;
         j->st.attempts = (uint64_t)attempt + 1;
@@ -1101,20 +1101,11 @@ static gx_status build_partitioned(RunCtx &rc) {
         CK(cudaEventRecord(tm.ev[5], s));
         launch_emit_write_part(a, s);
         CK(cudaEventRecord(tm.ev[6], s));
-        CK(d2h_async(&hs, rc.d_st, sizeof hs, s));
-        CK(sync_stream(s));
-        CK(cudaGetLastError());
-        if (hs.internal_err) {
-            cudaFreeAsync(outp, s);
-            cudaFreeAsync(part_off, s);
-            fprintf(stderr, "gxgpu: internal error: record sizes disagree between emission passes\n");
-            return GX_ECUDA;
-        }
         NodeRecords nr;
         nr.nkey = okey2;
         nr.noff = noff;
         nr.node_base = fine_off;
-        if ((e = finish_outputs(rc, P, total, part_off, part_nodes, head_cnt2, outp, &nr)) != GX_OK) return e;
+        if ((e = finish_outputs(rc, P, total, part_off, part_nodes, head_cnt2, outp, hs, &nr)) != GX_OK) return e;
         j->st.table_slots = (uint64_t)P * AGG_SLOTS;
         j->st.table_partitions = P;
         j->st.attempts = (uint64_t)attempt + 1;
