@@ -167,7 +167,8 @@ def dist_setup(args):
     if ws > 1:
         import torch.distributed as dist
         import torch
-        torch.cuda.set_device(local)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
     return ws, rank, local
 
@@ -183,7 +184,8 @@ def max_over_ranks(ws, v):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
