@@ -965,20 +965,21 @@ static gx_status build_partitioned(RunCtx &rc) {
             if (soff[S] != n_occ) return GX_ECUDA;
         }
         const uint32_t P = pp.P;
-        // CHUNK-sized pieces of every super bucket
-        std::vector<ulonglong2> chunks;
-        chunks.reserve(n_occ / CHUNK + S + 1);
-        uint64_t placed = 0;
+        // CHUNK-sized pieces of every super bucket: counted here, written on the device
+        std::vector<uint32_t> cbase(S + 1, 0);
+        uint64_t placed = 0, nc64 = 0;
         for (uint32_t q = 0; q < S; q++) {
             placed += scount[q];
-            for (unsigned long long st = 0; st < scount[q]; st += CHUNK) {
-                const unsigned long long len = std::min<unsigned long long>(CHUNK, scount[q] - st);
-                chunks.push_back(make_ulonglong2(soff[q] + st, ((unsigned long long)q << 32) | len));
-            }
+            cbase[q] = (uint32_t)nc64;
+            nc64 += (scount[q] + CHUNK - 1) / CHUNK;
         }
-        if (placed != n_occ) return GX_ECUDA;
-        const uint32_t n_chunks = (uint32_t)chunks.size();
+        if (placed != n_occ || nc64 > 0x7fffffffULL) return GX_ECUDA;
+        cbase[S] = (uint32_t)nc64;
+        const uint32_t n_chunks = (uint32_t)nc64;
+        uint32_t *d_scount, *d_cbase;
         if ((e = tar.alloc(d_chunks, std::max<uint32_t>(n_chunks, 1))) != GX_OK) return e;
+        if ((e = tar.alloc(d_scount, S)) != GX_OK) return e;
+        if ((e = tar.alloc(d_cbase, S + 1)) != GX_OK) return e;
         if ((e = tar.alloc(fine_cnt, P)) != GX_OK) return e;
         if ((e = tar.alloc(fine_off, P + 1)) != GX_OK) return e;
         if ((e = tar.alloc(fine_cur, P)) != GX_OK) return e;
@@ -1000,15 +1001,16 @@ static gx_status build_partitioned(RunCtx &rc) {
         void *part_off_v = nullptr;
         CK(cudaMallocAsync(&part_off_v, (P + 1) * sizeof(unsigned long long), s));
         part_off = (unsigned long long *)part_off_v;
-        if (n_chunks)
-            CK(cudaMemcpyAsync(d_chunks, chunks.data(), n_chunks * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
+        if (counted) CK(cudaMemcpyAsync(d_soff, soff.data(), (S + 1) * 8ull, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_scount, scount.data(), S * 4ull, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_cbase, cbase.data(), (S + 1) * 4ull, cudaMemcpyHostToDevice, s));
+        launch_make_chunks(d_soff, d_scount, d_cbase, S, d_chunks, s);
         CK(cudaMemsetAsync(fine_cnt, 0, P * 8ull, s));
         CK(cudaMemsetAsync(fine_cur, 0, P * 4ull, s));
         CK(cudaMemsetAsync(head_cnt, 0, P * 4ull, s));
         CK(cudaMemsetAsync(head_cur, 0, P * 4ull, s));
         if (counted) {
             // A2 into the counted offsets
-            CK(cudaMemcpyAsync(d_soff, soff.data(), (S + 1) * 8ull, cudaMemcpyHostToDevice, s));
             launch_scatter_super(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, S, d_soff, s_cur,
                                  okey, obits, 0xffffffffu, nullptr, nullptr, s);
         }

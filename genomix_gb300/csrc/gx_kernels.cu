@@ -1768,6 +1768,28 @@ void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const 
     }
 }
 
+// the CHUNK-sized pieces of each super bucket, (start, super << 32 | length), super by super:
+// bucket q's pieces are chunks[cbase[q] .. cbase[q + 1])
+__global__ void k_make_chunks(const unsigned long long *soff, const uint32_t *scount, const uint32_t *cbase,
+                              uint32_t S, ulonglong2 *chunks) {
+    for (uint32_t q = blockIdx.x; q < S; q += gridDim.x) {
+        const uint32_t c0 = cbase[q], nc = cbase[q + 1] - c0, cnt = scount[q];
+        const unsigned long long base = soff[q];
+        for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
+            const uint32_t st = c * CHUNK;
+            const uint32_t len = min(CHUNK, cnt - st);
+            chunks[c0 + c] = make_ulonglong2(base + st, ((unsigned long long)q << 32) | len);
+        }
+    }
+}
+
+void launch_make_chunks(const unsigned long long *soff, const uint32_t *scount, const uint32_t *cbase, uint32_t S,
+                        ulonglong2 *chunks, cudaStream_t s) {
+    if (!S) return;
+    t_launches++;
+    k_make_chunks<<<S, 256, 0, s>>>(soff, scount, cbase, S, chunks);
+}
+
 // ---- B1 -------------------------------------------------------------------------------------
 constexpr int FINE_PER_THREAD = CHUNK / 256;  // occurrences of a chunk per thread
 

@@ -157,6 +157,8 @@ void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const 
                           const unsigned long long *s_off, uint32_t *s_cur, void *okey, uint16_t *obits,
                           uint32_t cap, uint32_t *hll, uint32_t *ovf, cudaStream_t s);
 // chunks: (start, super << 32 | length) of CHUNK-sized pieces of each super bucket
+void launch_make_chunks(const unsigned long long *soff, const uint32_t *scount, const uint32_t *cbase, uint32_t S,
+                        ulonglong2 *chunks, cudaStream_t s);
 void launch_fine_count(int wide, const void *okey, const ulonglong2 *chunks, uint32_t n_chunks,
                        const SuperInfo *sinfo, unsigned long long *fine_cnt, cudaStream_t s);
 void launch_scatter_fine(int wide, const void *okey, const uint16_t *obits, const ulonglong2 *chunks,
