@@ -125,7 +125,7 @@ class ClockSampler:
                     self.first.set()
             self.thread = threading.Thread(target=reader, daemon=True)
             self.thread.start()
-            # nvidia-smi's start-up talks to the driver: let it finish before the timed region
+            # nvidia-smi's start-up queries the GPU through the NVIDIA kernel module: let it finish first
             self.first.wait(timeout=10)
             time.sleep(0.25)
         return self
