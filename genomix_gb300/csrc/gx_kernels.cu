@@ -3175,8 +3175,10 @@ __global__ void __launch_bounds__(256) k_rl_move(const uint8_t *sbytes, Src src,
         for (uint32_t m = same & ((1u << lane) - 1u); m; m &= m - 1) pre += slen[warp * 32 + __ffs(m) - 1];
         if (live && (same >> lane) == 1u) wb[warp][d] = (unsigned long long)pre + len;  // the group's last lane
         // the round's source range; its loads go out first
-        const uint32_t cnt = min(256u, n - j0);
-        const unsigned long long lo = ssrc[0] & ~15ull, hi = (ssrc[cnt - 1] + slen[cnt - 1] + 15) & ~15ull;
+        // records this round; an empty bucket (no nodes) still takes one round, with nothing to move
+        const uint32_t cnt = n > j0 ? min(256u, n - j0) : 0u;
+        const unsigned long long lo = cnt ? ssrc[0] & ~15ull : 0ull;
+        const unsigned long long hi = cnt ? (ssrc[cnt - 1] + slen[cnt - 1] + 15) & ~15ull : 0ull;
         const bool fits = hi - lo <= (unsigned long long)RL_STAGE;
         if (fits) {
             const uint32_t span = (uint32_t)(hi - lo);
