@@ -889,11 +889,29 @@ static gx_status build_partitioned(RunCtx &rc) {
         HeadOut *hout;
         uint32_t *noff;
         uint8_t *okey_b, *okey2_b;
-        if ((e = tar.alloc(okey_b, occ_room * kb)) != GX_OK) return e;
+        // The room per bucket of the uncounted scatter costs (occ_room - n_occ) x (kb + 2) bytes
+        // more than the exact counts: when that does not fit (the context's limit, or a failed
+        // allocation), count first and scatter into the exact offsets instead.
+        if (!counted) {
+            const double need = (double)(occ_room + n_occ) * (double)(kb + 2) + (double)n_occ * 4.0 +
+                                (double)n_reads * (sizeof(Head) + sizeof(HeadOut) + 12.0);
+            bool fits = need <= (double)j->ctx->mem_limit;
+            if (fits) fits = tar.alloc(okey_b, occ_room * kb) == GX_OK && tar.alloc(obits, occ_room) == GX_OK;
+            if (!fits) {
+                tar.release();
+                if ((e = count_supers(rc)) != GX_OK) return e;
+                counted = true;
+                d_est = hll_estimate(rc.hll.data());
+                attempt--;
+                continue;
+            }
+        } else {
+            if ((e = tar.alloc(okey_b, occ_room * kb)) != GX_OK) return e;
+            if ((e = tar.alloc(obits, occ_room)) != GX_OK) return e;
+        }
         if ((e = tar.alloc(okey2_b, n_occ * kb)) != GX_OK) return e;
         okey = okey_b;
         okey2 = okey2_b;
-        if ((e = tar.alloc(obits, occ_room)) != GX_OK) return e;
         if ((e = tar.alloc(obits2, n_occ)) != GX_OK) return e;
         if ((e = tar.alloc(d_soff, S + 1)) != GX_OK) return e;
         if ((e = tar.alloc(s_cur, S)) != GX_OK) return e;

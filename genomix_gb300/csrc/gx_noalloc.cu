@@ -68,13 +68,31 @@ gx_status too_big(const char *what) {
 
 }  // namespace
 
+// The build proper; the caller has made `device` current.
+static gx_status build_noalloc(int device, const void *text_dev, size_t n_text, int k, void *out_dev, size_t out_cap,
+                               size_t *out_bytes);
+
 extern "C" gx_status gx_build_noalloc(int device, const void *text_dev, size_t n_text, int k, void *out_dev,
                                       size_t out_cap, size_t *out_bytes) {
     if (!out_bytes || (!text_dev && n_text) || k < 3 || k > 64 || device < 0 || device >= MAX_DEVICES)
         return GX_EINVAL;
     if (((uintptr_t)text_dev & 15) != 0 || (out_dev && ((uintptr_t)out_dev & 15) != 0)) return GX_EINVAL;
     *out_bytes = 0;
+    // the caller's current device is put back on every return: a JVM thread, for one, keeps
+    // using the device it had chosen
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+        cudaGetLastError();
+        prev = -1;
+    }
     if (cudaSetDevice(device) != cudaSuccess) return GX_ECUDA;
+    const gx_status st = build_noalloc(device, text_dev, n_text, k, out_dev, out_cap, out_bytes);
+    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    return st;
+}
+
+static gx_status build_noalloc(int device, const void *text_dev, size_t n_text, int k, void *out_dev, size_t out_cap,
+                               size_t *out_bytes) {
     void *scratch_base;
     {
         std::lock_guard<std::mutex> lk(g_mu);
@@ -129,61 +147,74 @@ extern "C" gx_status gx_build_noalloc(int device, const void *text_dev, size_t n
     if (hs.parse_err != ~0ULL) return (gx_status)(hs.parse_err & 0xff);
     if (n_reads == 0) return GX_OK;
 
-    // ---- table build: the geometry gx_job_run uses at the default fill (0.5) ----
-    const uint64_t want = (uint64_t)((double)hs.n_occ / 0.5) + 1;
-    const uint32_t nparts = (uint32_t)std::max<uint64_t>(1, (want + PART_SLOTS - 1) / PART_SLOTS);
-    const size_t slot_bytes = wide ? sizeof(Slot128) : sizeof(Slot64);
-    const size_t table_bytes = (size_t)nparts * PART_SLOTS * slot_bytes;
-    unsigned char *table;
-    Head *heads;
-    uint32_t *head_cnt, *head_off, *head_cur, *head_idx, *head_cnt2, *part_nodes;
-    unsigned long long *head_sk, *part_bytes, *part_off;
-    void *pscratch;
-    if (!ar.take(table, table_bytes) || !ar.take(heads, n_reads) || !ar.take(head_cnt, nparts) ||
-        !ar.take(head_off, nparts) || !ar.take(head_cur, nparts) || !ar.take(head_idx, n_reads) ||
-        !ar.take(head_cnt2, nparts) || !ar.take(head_sk, n_reads) || !ar.take(part_nodes, nparts) ||
-        !ar.take(part_bytes, nparts) || !ar.take(part_off, nparts + 1) ||
-        !ar.take(pscratch, scan_scratch_bytes(nparts, 8)))
-        return too_big("hash table");
-    // everything that must start at zero
-    NA_CK(cudaMemsetAsync(table, 0, table_bytes, s));
-    NA_CK(cudaMemsetAsync(head_cnt, 0, nparts * 4ull, s));
-    NA_CK(cudaMemsetAsync(head_cur, 0, nparts * 4ull, s));
-    TableGeom g{table, nparts, wide};
-    launch_insert(g, text, lines, reads, n_reads, k, heads, head_cnt, d_st, s);
-    exclusive_scan_u32(head_cnt, head_off, nparts, nullptr, pscratch, s);
-    launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, nparts, s);
-    EmitArgs a{};
-    a.g = g;
-    a.k = k;
-    a.text = text;
-    a.lines = lines;
-    a.reads = reads;
-    a.heads = heads;
-    a.head_idx = head_idx;
-    a.head_sk = head_sk;
-    a.head_off = head_off;
-    a.head_cnt = head_cnt;
-    a.head_cnt2 = head_cnt2;
-    a.part_nodes = part_nodes;
-    a.part_bytes = part_bytes;
-    a.part_off = part_off;
-    a.st = d_st;
-    launch_emit_prepare(a, s);
-    exclusive_scan_u64(part_bytes, part_off, nparts, part_off + nparts, pscratch, s);
-    unsigned long long total = 0;
-    NA_CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-    NA_CK(cudaMemcpyAsync(&total, part_off + nparts, 8, cudaMemcpyDeviceToHost, s));
-    NA_CK(cudaStreamSynchronize(s));
-    NA_CK(cudaGetLastError());
-    if (hs.table_full) return GX_ETABLE_FULL;
-    *out_bytes = total;
-    if (!out_dev || total > out_cap) return GX_EINVAL;  // *out_bytes tells the size needed
-    a.out = (uint8_t *)out_dev;
-    launch_emit_write(a, s);
-    NA_CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
-    NA_CK(cudaStreamSynchronize(s));
-    NA_CK(cudaGetLastError());
-    if (hs.internal_err) return GX_ECUDA;
-    return GX_OK;
+    // ---- table build: the geometry gx_job_run uses at the default fill (0.5); a partition
+    //      that overflows retries at half the fill, up to three attempts, as gx_job_run does
+    const size_t mark = ar.used;
+    double lf = 0.5;
+    for (int attempt = 0;; attempt++, lf *= 0.5) {
+        ar.used = mark;
+        const uint64_t want = (uint64_t)((double)hs.n_occ / lf) + 1;
+        const uint32_t nparts = (uint32_t)std::max<uint64_t>(1, (want + PART_SLOTS - 1) / PART_SLOTS);
+        const size_t slot_bytes = wide ? sizeof(Slot128) : sizeof(Slot64);
+        const size_t table_bytes = (size_t)nparts * PART_SLOTS * slot_bytes;
+        unsigned char *table;
+        Head *heads;
+        uint32_t *head_cnt, *head_off, *head_cur, *head_idx, *head_cnt2, *part_nodes;
+        unsigned long long *head_sk, *part_bytes, *part_off;
+        void *pscratch;
+        if (!ar.take(table, table_bytes) || !ar.take(heads, n_reads) || !ar.take(head_cnt, nparts) ||
+            !ar.take(head_off, nparts) || !ar.take(head_cur, nparts) || !ar.take(head_idx, n_reads) ||
+            !ar.take(head_cnt2, nparts) || !ar.take(head_sk, n_reads) || !ar.take(part_nodes, nparts) ||
+            !ar.take(part_bytes, nparts) || !ar.take(part_off, nparts + 1) ||
+            !ar.take(pscratch, scan_scratch_bytes(nparts, 8)))
+            return too_big("hash table");
+        // everything that must start at zero
+        NA_CK(cudaMemsetAsync(table, 0, table_bytes, s));
+        NA_CK(cudaMemsetAsync(head_cnt, 0, nparts * 4ull, s));
+        NA_CK(cudaMemsetAsync(head_cur, 0, nparts * 4ull, s));
+        TableGeom g{table, nparts, wide};
+        launch_insert(g, text, lines, reads, n_reads, k, heads, head_cnt, d_st, s);
+        exclusive_scan_u32(head_cnt, head_off, nparts, nullptr, pscratch, s);
+        launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, nparts, s);
+        EmitArgs a{};
+        a.g = g;
+        a.k = k;
+        a.text = text;
+        a.lines = lines;
+        a.reads = reads;
+        a.heads = heads;
+        a.head_idx = head_idx;
+        a.head_sk = head_sk;
+        a.head_off = head_off;
+        a.head_cnt = head_cnt;
+        a.head_cnt2 = head_cnt2;
+        a.part_nodes = part_nodes;
+        a.part_bytes = part_bytes;
+        a.part_off = part_off;
+        a.st = d_st;
+        launch_emit_prepare(a, s);
+        exclusive_scan_u64(part_bytes, part_off, nparts, part_off + nparts, pscratch, s);
+        unsigned long long total = 0;
+        NA_CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
+        NA_CK(cudaMemcpyAsync(&total, part_off + nparts, 8, cudaMemcpyDeviceToHost, s));
+        NA_CK(cudaStreamSynchronize(s));
+        NA_CK(cudaGetLastError());
+        if (hs.table_full) {
+            if (attempt >= 2) return GX_ETABLE_FULL;
+            DevStatus again{};
+            again.parse_err = ~0ULL;
+            again.n_occ = hs.n_occ;
+            NA_CK(cudaMemcpyAsync(d_st, &again, sizeof again, cudaMemcpyHostToDevice, s));
+            continue;
+        }
+        *out_bytes = total;
+        if (!out_dev || total > out_cap) return GX_EINVAL;  // *out_bytes tells the size needed
+        a.out = (uint8_t *)out_dev;
+        launch_emit_write(a, s);
+        NA_CK(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
+        NA_CK(cudaStreamSynchronize(s));
+        NA_CK(cudaGetLastError());
+        if (hs.internal_err) return GX_ECUDA;
+        return GX_OK;
+    }
 }

@@ -343,8 +343,13 @@ void gx_serve_destroy(gx_server *srv);
  * 16-byte aligned) and a device output buffer (16-byte aligned, out_cap bytes) that
  * receives the same record stream gx_job_run writes with algorithm GX_ALGO_TABLE.
  *  - The first call on a device looks up the array's device address with that device
- *    current; make that first call before any stream capture.
- *  - Work runs on the legacy default stream of `device`; the call returns when it is done.
+ *    current; make that first call before any stream capture.  The address is kept for the
+ *    life of the process: after a cudaDeviceReset of that device this call must not be used
+ *    on it again.
+ *  - Work runs on the legacy default stream of `device`; the call returns when it is done,
+ *    with the caller's current device as it was before the call.
+ *  - A hash-table partition that overflows is retried at half the fill, up to three
+ *    attempts, as gx_job_run's table build does; GX_ETABLE_FULL after the third.
  *  - Calls share the one array (each starts by clearing what must start at zero): calls
  *    that overlap on the GPU, from different host threads, race and must not be made.
  *  - An input whose working set does not fit the array returns GX_ENOMEM with a message

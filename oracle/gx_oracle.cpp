@@ -550,6 +550,12 @@ struct Parser {
     KmerOps ko;
     TupleStore &out;
     ParseStats st;
+    // Only the tuples whose key the reference's partitioner sends to part keep_part of keep_of
+    // are stored (keep_part < 0: all).  Every occurrence of a key goes to the same part, so the
+    // parts built one at a time hold exactly the records of the whole build, with the memory of
+    // one part: this is how whole benchmark-size inputs are checked.
+    int keep_part = -1, keep_of = 1;
+    bool kept(const uint8_t *key) const { return keep_part < 0 || kmer_partition(key, ko.nb, keep_of) == keep_part; }
 
     Parser(int k, TupleStore &o) : out(o) {
         ko.k = k;
@@ -607,7 +613,11 @@ struct Parser {
                    const std::vector<uint8_t> &curR, const std::vector<uint8_t> &nextF,
                    const std::vector<uint8_t> &nextR) {
         const int k = ko.k, nb = ko.nb;
+        // an edge of a node that is not stored changes no output (the skip only saves time)
+        const bool keep_cur = keep_part < 0 || kept(cd == FORWARD ? curF.data() : curR.data());
+        const bool keep_next = keep_part < 0 || kept(nd == FORWARD ? nextF.data() : nextR.data());
         auto app = [&](Node &n, int e, const std::vector<uint8_t> &km) {
+            if (&n == &cur ? !keep_cur : !keep_next) return;
             n.has_edges[e] = true;
             n.edges[e].push_back(vkmer_from_kmer(k, km.data(), nb));
         };
@@ -628,6 +638,7 @@ struct Parser {
 
     // writeToFrame / InsertToFrame (ReadsKeyValueParserFactory.java:198-254)
     void write_to_frame(const std::vector<uint8_t> &f, const std::vector<uint8_t> &r, DIR d, const Node &n) {
+        if (!kept(d == FORWARD ? f.data() : r.data())) return;
         std::string v;
         write_node(v, n);
         out.add(d == FORWARD ? f.data() : r.data(), ko.nb, v);
@@ -732,9 +743,10 @@ static void append_record(std::string &o, int k, const std::string &kmer, const 
 }
 
 // The whole job.  threads = input splits = partitions (one NC partition per thread).
-static Result build(const uint8_t *text, size_t n, int k, int threads, int parts) {
+// only_part >= 0: build only the records of that part (the others stay empty).
+static Result build(const uint8_t *text, size_t n, int k, int threads, int parts, int only_part = -1) {
     Result res;
-    if (k < 3 || threads < 1 || parts < 1) {
+    if (k < 3 || threads < 1 || parts < 1 || only_part >= parts) {
         res.status = GX_EINVAL;
         return res;
     }
@@ -751,6 +763,8 @@ static Result build(const uint8_t *text, size_t n, int k, int threads, int parts
         size_t a = lines.size() * (size_t)t / T, b = lines.size() * (size_t)(t + 1) / T;
         TupleStore ts;
         Parser ps(k, ts);
+        ps.keep_part = only_part;
+        ps.keep_of = P;
         for (size_t i = a; i < b; i++) {
             int e = ps.parse(text + lines[i].begin, lines[i].end - lines[i].begin);
             if (e != GX_OK) {
@@ -1054,6 +1068,9 @@ static int fastq_to_readid(const uint8_t *m1, size_t n1, const uint8_t *m2, size
 // =======================================================================================
 extern "C" {
 
+struct gxo_result;
+int gxo_build_part(const char *text, size_t n, int k, int threads, int parts, int part, gxo_result **out);
+
 struct gxo_result {
     gxo::Result r;
     std::string all;  // parts concatenated in partition order
@@ -1064,8 +1081,15 @@ struct gxo_result {
 // output partitions.  Returns the status; *out always receives a handle (free with
 // gxo_result_free).
 int gxo_build(const char *text, size_t n, int k, int threads, int parts, gxo_result **out) {
+    return gxo_build_part(text, n, k, threads, parts, -1, out);
+}
+
+// The same build keeping only the records of part `part` of `parts` (the reference's
+// partitioner, KmerPartitionComputerFactory.java:28-52); part -1 keeps every part.  The
+// statistics other than nodes and heads are those of the whole input.
+int gxo_build_part(const char *text, size_t n, int k, int threads, int parts, int part, gxo_result **out) {
     gxo_result *h = new gxo_result();
-    h->r = gxo::build((const uint8_t *)text, n, k, threads, parts);
+    h->r = gxo::build((const uint8_t *)text, n, k, threads, parts, part);
     h->part_off.push_back(0);
     for (auto &p : h->r.parts) {
         h->all += p;

@@ -33,6 +33,9 @@ def lib():
         L.gxo_build.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                 ctypes.POINTER(ctypes.c_void_p)]
         L.gxo_build.restype = ctypes.c_int
+        L.gxo_build_part.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        L.gxo_build_part.restype = ctypes.c_int
         L.gxo_result_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
         L.gxo_result_records.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]
         L.gxo_result_records.restype = ctypes.c_void_p
@@ -73,11 +76,13 @@ class OracleResult:
         self.part_offsets = part_offsets
 
 
-def build_graph(text: bytes, k: int, threads: int = 1, parts: int = 1) -> OracleResult:
-    """Runs the oracle graph build over readid text; returns status, stats and records."""
+def build_graph(text: bytes, k: int, threads: int = 1, parts: int = 1, only_part: int = -1) -> OracleResult:
+    """Runs the oracle graph build over readid text; returns status, stats and records.
+    only_part >= 0 keeps only the records of that part of `parts` (the reference's Kmer
+    partitioner): the parts built one at a time add up to the whole build, in the memory of one."""
     L = lib()
     h = ctypes.c_void_p()
-    st = L.gxo_build(text, len(text), k, threads, parts, ctypes.byref(h))
+    st = L.gxo_build_part(text, len(text), k, threads, parts, only_part, ctypes.byref(h))
     stats = (ctypes.c_uint64 * 6)()
     L.gxo_result_stats(h, stats)
     n = ctypes.c_size_t()

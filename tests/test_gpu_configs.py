@@ -3,13 +3,17 @@
 Bit-exact against the oracle where the oracle finishes in seconds: all of the plain CPU-sized
 workload (10,000 single-end reads, k = 21), prefixes of the 5 Mbp paired-end (k = 31) and
 50 Mbp long-k (k = 55) workloads, shrunken samples of the 64-sample batch and of the served
-stream.  At full size, through size-independent properties: the partitioned build, the
+stream, and at full size the 5 Mbp workload in all its records and the 50 Mbp workload in a
+seeded 5 % of them (one part of the reference part layout at a time).  At full size, also
+through size-independent properties: the partitioned build, the
 global-table build and the batched build of the same reads give the same order-independent
 digest of their normalised records, the coverage of all nodes sums to the k-mer occurrences,
 the read heads to the valid mates (no read id repeats in these workloads), and the digest
 counts agree with the build's own statistics.
 """
 import multiprocessing as mp
+import os
+import random
 from concurrent.futures import ProcessPoolExecutor
 
 import pytest
@@ -105,6 +109,59 @@ def check_full_size(ctx, w, parts):
     return stats, d
 
 
+def part_digest(job, q, buf, cap):
+    """Digest of output part q of a job, streamed through a pinned buffer."""
+    tot = {"records": 0, "edges": 0, "heads": 0, "coverage": 0, "sum": 0, "xor_": 0}
+    job.rewind(q)
+    while True:
+        w, more = job.emit_into(q, buf.ptr, cap)
+        if w:
+            d = gx.records_digest(buf.ptr, w)
+            for f in ("records", "edges", "heads", "coverage"):
+                tot[f] += d[f]
+            tot["sum"] = (tot["sum"] + d["sum"]) & ((1 << 64) - 1)
+            tot["xor_"] ^= d["xor_"]
+        if not more:
+            return tot
+
+
+def check_parts_vs_oracle(ctx, w, parts, which, full_bytes_part=None):
+    """The whole-size build against the oracle, one part at a time: the GPU build writes its
+    records in the reference's part layout (the reference's Kmer partitioner), and the oracle
+    builds only the records of one part per run, so host memory holds one part.  Every part in
+    `which` must carry the same digest (records, edges, heads, coverage and the record-hash sum
+    and xor) as the oracle's part of the same number; part `full_bytes_part` is also compared
+    byte for byte in normal form."""
+    threads = os.cpu_count() or 8
+    job = gx.GraphBuildJob(ctx, w.k, out_parts=parts, layout="reference")
+    job.add_input(w.text)
+    job.run()
+    st = job.stats()
+    offs = job.part_offsets()
+    cap = max(offs[q + 1] - offs[q] for q in range(parts)) + 16
+    buf = gx.PinnedBuffer(cap)
+    nodes = 0
+    try:
+        for q in which:
+            ref = go.build_graph(w.text, w.k, threads=threads, parts=parts, only_part=q)
+            assert ref.status == 0
+            assert (ref.kmers, ref.reads) == (st["kmers"], st["reads"])
+            got = part_digest(job, q, buf, cap)
+            assert got == gx.records_digest(ref.records), f"part {q} of {parts}"
+            if q == full_bytes_part:
+                job.rewind(q)
+                w_, more = job.emit_into(q, buf.ptr, cap)
+                assert not more
+                mine = bytes(buf.array()[:w_])
+                assert go.normalize(mine) == go.normalize(ref.records), f"part {q} bytes"
+            nodes += ref.nodes
+            del ref
+    finally:
+        buf.close()
+        job.close()
+    return st, nodes
+
+
 # ---- configuration 1: 50 kbp genome, 10,000 x 100 bp single-end, k = 21 --------------------
 def test_plain_cpu_workload_vs_oracle(ctx):
     w = synth.plain_cpu()
@@ -123,6 +180,15 @@ def test_pe_5mbp_full_size_properties(ctx):
     assert stats["kmers"] == 197_007_720 and stats["reads"] == 1_641_731
 
 
+def test_pe_5mbp_full_size_vs_oracle(ctx):
+    """Every record of the benchmarked build (197,007,720 occurrences) against the oracle: all
+    four parts of the reference part layout, part 0 byte for byte in normal form."""
+    w = synth.pe_5mbp()
+    st, nodes = check_parts_vs_oracle(ctx, w, 4, range(4), full_bytes_part=0)
+    assert st["kmers"] == 197_007_720
+    assert nodes == st["nodes"]
+
+
 # ---- configuration 3: 50 Mbp, 2 x 250 bp pairs, k = 55 (128-bit keys) ------------------------
 def test_pe_50mbp_prefix_vs_oracle(ctx, pool):
     check_vs_oracle(ctx, synth.pe_50mbp(max_pairs=5_000, pool=pool).text, 55)
@@ -133,6 +199,14 @@ def test_pe_50mbp_full_size_properties(ctx, pool):
     assert w.reads == 2_000_000
     stats, d = check_full_size(ctx, w, parts=16)
     assert stats["key_bits"] == 128
+
+
+def test_pe_50mbp_full_size_sampled_parts_vs_oracle(ctx, pool):
+    """The 784 M-occurrence long-k build against the oracle on a seeded 5 % of its records: one
+    part of 20 of the reference part layout (the oracle over every part would take minutes)."""
+    w = synth.pe_50mbp(pool=pool)
+    q = random.Random(20261204).randrange(20)
+    check_parts_vs_oracle(ctx, w, 20, [q], full_bytes_part=q)
 
 
 # ---- configuration 4: the 64-sample batch ---------------------------------------------------

@@ -300,3 +300,20 @@ def test_super_bucket_overflow_falls_back_to_counting(ctx):
         job.close()
         assert (st["nodes"], st["kmers"], st["read_heads"]) == (ref.nodes, ref.kmers, ref.read_heads)
         assert go.normalize(rec) == go.normalize(ref.records)
+
+
+def test_memory_limit_between_counted_and_uncounted_scatter():
+    """A context whose memory limit holds the exact-count build but not the uncounted scatter's
+    room per bucket (about 1.3 x the occurrences): the build counts first instead of failing,
+    and its records are the oracle's."""
+    text = synth.pe_5mbp(max_pairs=20_000).text
+    ref = go.build_graph(text, 31, threads=8, parts=2)
+    with gx.Context(0) as c:
+        _, base = gpu_build(c, text, 31, algorithm="partitioned")
+    n_occ = base["kmers"]
+    # the uncounted pass asks for about 23 B per occurrence, the counted one for about 14
+    with gx.Context(0, mem_limit=int(19 * n_occ)) as c:
+        rec, st = gpu_build(c, text, 31, algorithm="partitioned")
+    assert st["kernel_launches"] > base["kernel_launches"]  # the counting pass ran
+    assert (st["nodes"], st["kmers"], st["read_heads"]) == (ref.nodes, ref.kmers, ref.read_heads)
+    assert go.normalize(rec) == go.normalize(ref.records)

@@ -11,12 +11,13 @@ import pytest
 
 import genomix_gb300 as gx
 from genomix_gb300 import _lib, synth
+from oracle import gx_oracle as go
 
 pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
 
-GX_EINVAL, GX_ENOMEM = 1, 6  # gx_status values from include/gxgpu.h
+GX_EINVAL, GX_EINVAL_LINE, GX_ENOMEM = 1, 2, 6  # gx_status values from include/gxgpu.h
 
 
 def job_records(text, k):
@@ -57,6 +58,32 @@ def test_noalloc_matches_job_run_twice(k):
         assert bool((out[n:] == 0xAB).all())  # nothing written past the records
         outs.append(got)
     assert outs[0] == outs[1]
+    # and the records are the oracle's
+    oref = go.build_graph(text, k, threads=4, parts=2)
+    assert oref.status == 0
+    assert go.normalize(outs[0]) == go.normalize(oref.records)
+
+
+def test_noalloc_after_parse_error_and_keeps_device():
+    """A call that stops on a parse error leaves its status and counters in the shared array;
+    the next call must clear them and give the same records as gx_job_run.  The caller's current
+    device is the same after every call."""
+    L = _lib.load()
+    k = 31
+    good = synth.plain_cpu(max_reads=3000).text
+    ref, _ = job_records(good, k)
+    bad = torch.frombuffer(bytearray(b"2\tACGTACGTACGTACGTACGTACGTACGTACGTACGT\n6\n"), dtype=torch.uint8).cuda()
+    t = torch.frombuffer(bytearray(good), dtype=torch.uint8).cuda()
+    out = torch.empty(len(ref) + 64, dtype=torch.uint8, device="cuda")
+    before = torch.cuda.current_device()
+    status, _ = noalloc(L, bad.data_ptr(), bad.numel(), k, out.data_ptr(), out.numel())
+    assert status == GX_EINVAL_LINE
+    assert torch.cuda.current_device() == before
+    for _ in range(2):
+        status, n = noalloc(L, t.data_ptr(), t.numel(), k, out.data_ptr(), out.numel())
+        assert status == _lib.GX_OK, _lib.status_str(status)
+        assert out[:n].cpu().numpy().tobytes() == ref
+    assert torch.cuda.current_device() == before
 
 
 def test_noalloc_size_query_and_limits():
