@@ -127,7 +127,7 @@ class Stats(ctypes.Structure):
         ("kernel_launches", ctypes.c_uint64),
         ("ms_parse", ctypes.c_double), ("ms_insert", ctypes.c_double), ("ms_emit", ctypes.c_double),
         ("ms_total", ctypes.c_double), ("ms_aggregate", ctypes.c_double), ("ms_write", ctypes.c_double),
-        ("attempts", ctypes.c_uint64), ("ms_layout", ctypes.c_double),
+        ("attempts", ctypes.c_uint64), ("ms_layout", ctypes.c_double), ("super_counted", ctypes.c_uint64),
     ]
 
     def as_dict(self):

@@ -1128,6 +1128,7 @@ static gx_status build_partitioned(RunCtx &rc) {
         if ((e = finish_outputs(rc, P, total, part_off, part_nodes, head_cnt2, outp, hs, &nr)) != GX_OK) return e;
         j->st.table_slots = (uint64_t)P * AGG_SLOTS;
         j->st.table_partitions = P;
+        j->st.super_counted = counted ? 1 : 0;
         j->st.attempts = (uint64_t)attempt + 1;
         j->st.max_probe = 0;
         j->st.cov_inexact_nodes = hs.cov_inexact;

@@ -306,7 +306,7 @@ void launch_write_lines(const uint8_t *text, uint64_t n, const uint32_t *tile_of
 }
 
 // =========================================================================================
-// K1b: per-line parse, one warp per line.  Reproduces, in order, the checks of
+// K1b: per-line parse, one thread per line.  Reproduces, in order, the checks of
 // ReadsKeyValueParserFactory.parse (:95-148) and SplitReads (:152-155):
 //   value.toString().split("\\t") must give 2 or 3 fields   -> GX_EINVAL_LINE
 //   Long.parseLong(field 0)                                 -> GX_EINVAL_NUMBER
@@ -363,173 +363,130 @@ __device__ __forceinline__ uint32_t bit_range(long long lo, long long hi) {
     return top & ~((1u << (uint32_t)lo) - 1u);
 }
 
-constexpr int PARSE_SPAN = 32;                  // text bytes per lane per step
-constexpr int PARSE_STEP = 32 * PARSE_SPAN;     // bytes per warp step
-constexpr int PARSE_KEEP = 2;                   // steps whose letter masks stay in registers
-
-// tab and non-ACGT masks of the 32 bytes at `base` (16-byte aligned), limited to [b, e)
-__device__ __forceinline__ void classify_span(const uint8_t *text, uint64_t n_text, uint64_t base, uint64_t b,
-                                              uint64_t e, uint32_t &tm, uint32_t &nt, uint32_t &bm) {
-    tm = nt = bm = 0;
-    if (base >= e) return;
-    uint32_t tab = 0, bad = 0;
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        uint32_t wd[4];
-        load16(text, n_text, base + 16 * h, wd);
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            uint32_t t4, b4;
-            classify_word(wd[q], t4, b4);
-            tab |= t4 << (16 * h + 4 * q);
-            bad |= b4 << (16 * h + 4 * q);
-        }
-    }
-    const uint32_t im = bit_range((long long)b - (long long)base, (long long)e - (long long)base);
-    tm = tab & im;
-    nt = im & ~tm;
-    bm = bad & nt;
-}
-
+// One thread per line.  The thread reads its line in 16-byte loads (two in flight) and
+// classifies four bytes per word operation: tab bytes, bytes outside [ACGTacgt], the last
+// non-tab byte.  Words without a tab (all but two or three per line) cost a few operations;
+// a word holding a tab is walked byte by byte to place the tab and split the field marks.
 __global__ void __launch_bounds__(256) k_parse_lines(const uint8_t *text, uint64_t n_text,
                                                      const unsigned long long *line_end, uint32_t n_lines, int k,
                                                      LineRec *lines, uint8_t *lflags, uint32_t *nvalid,
                                                      DevStatus *st) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t warp0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t line = warp0; line < n_lines; line += nwarps) {
-        const uint64_t b = line == 0 ? 0 : line_end[line - 1] + 1;
-        uint64_t e = line_end[line];
-        if (e < n_text && e > b && text[e] == '\n' && text[e - 1] == '\r') e--;
-        const uint32_t len = (uint32_t)(e - b);
+    const uint64_t line = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= n_lines) return;
+    const uint64_t b = line == 0 ? 0 : line_end[line - 1] + 1;
+    uint64_t e = line_end[line];
+    if (e < n_text && e > b && text[e] == '\n' && text[e - 1] == '\r') e--;
+    const uint32_t len = (uint32_t)(e - b);
 
-        // one pass: tab positions (the first three, and how many), the last non-tab byte,
-        // and the bytes outside [ACGTacgt] (kept for the first PARSE_KEEP steps)
-        uint32_t tab[3] = {len, len, len};
-        uint32_t found = 0, tabs = 0;
-        int last_nt = -1;
-        uint32_t keep_bm[PARSE_KEEP] = {0u, 0u};
-        const uint64_t c0 = b & ~15ULL;
-        uint32_t step = 0;
-        for (uint64_t w = c0; w < e; w += PARSE_STEP, step++) {
-            const uint64_t base = w + (uint64_t)PARSE_SPAN * lane;
-            uint32_t tm, nt, bm;
-            classify_span(text, n_text, base, b, e, tm, nt, bm);
-            if (step < PARSE_KEEP) keep_bm[step] = bm;
-            const uint32_t cl = __popc(tm);
-            const uint32_t incl = warp_inclusive_scan(cl);
-            const uint32_t pre = incl - cl;
-            const uint32_t wt = __shfl_sync(0xffffffffu, incl, 31);
-            for (uint32_t r = found; r < 3 && r < found + wt; r++) {
-                const uint32_t rr = r - found;
-                const bool own = rr >= pre && rr < incl;
-                const uint32_t om = __ballot_sync(0xffffffffu, own);
-                uint32_t pos = 0;
-                if (own) {
-                    uint32_t m = tm;
-                    for (uint32_t i = 0; i < rr - pre; i++) m &= m - 1;
-                    pos = (uint32_t)(base + (__ffs(m) - 1) - b);
-                }
-                tab[r] = __shfl_sync(0xffffffffu, pos, __ffs(om) - 1);
-            }
-            found = min(3u, found + wt);
-            tabs += wt;
-            const int lnt = nt ? (int)(base + 31 - __clz(nt) - b) : -1;
-            last_nt = max(last_nt, __reduce_max_sync(0xffffffffu, lnt));
-        }
-        // String.split: trailing empty fields removed; no tab at all gives one field
-        int nf;
-        if (tabs == 0)
-            nf = 1;
-        else if (last_nt < 0)
-            nf = 0;
+    // tabs: where the first three are and how many; the last non-tab byte; which of fields 1
+    // and 2 hold a byte outside [ACGTacgt] (bit f of badf)
+    uint32_t tabs = 0, t0 = len, t1 = len, t2 = len, field = 0, badf = 0;
+    long long last_nt = -1;
+    for (uint64_t c = b & ~15ULL; c < e; c += 32) {
+        uint32_t wd[8];
+        load16(text, n_text, c, wd);
+        if (c + 16 < e)
+            load16(text, n_text, c + 16, wd + 4);
         else
-            nf = 1 + (int)tabs - (int)(len - 1 - (uint32_t)last_nt);
-
-        // field ranges (relative to b)
-        const uint32_t f1b = tab[0] + 1, f1e = tabs >= 2 ? tab[1] : len;
-        const uint32_t f2b = tab[1] + 1, f2e = tabs >= 3 ? tab[2] : len;
-        bool bad1 = false, bad2 = false;
-        if (nf == 2 || nf == 3) {
-            // [ACGTacgt]+ over fields 1 and 2, from the kept masks (a longer line reads the
-            // rest of its text again)
-            bool lb1 = false, lb2 = false;
-            step = 0;
-            for (uint64_t w = c0; w < e; w += PARSE_STEP, step++) {
-                const uint64_t base = w + (uint64_t)PARSE_SPAN * lane;
-                uint32_t bm;
-                if (step < PARSE_KEEP) {
-                    bm = keep_bm[step];
-                } else {
-                    uint32_t tm, nt;
-                    classify_span(text, n_text, base, b, e, tm, nt, bm);
-                }
-                const long long rel = (long long)base - (long long)b;
-                lb1 |= (bm & bit_range((long long)f1b - rel, (long long)f1e - rel)) != 0;
-                if (nf == 3) lb2 |= (bm & bit_range((long long)f2b - rel, (long long)f2e - rel)) != 0;
+            wd[4] = wd[5] = wd[6] = wd[7] = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const uint64_t p = c + 4 * q;
+            const uint32_t vm = bit_range((long long)b - (long long)p, (long long)e - (long long)p) & 15u;
+            if (!vm) continue;
+            uint32_t t4, b4;
+            classify_word(wd[q], t4, b4);
+            t4 &= vm;
+            b4 &= vm;
+            const uint32_t nt4 = vm & ~t4;
+            if (nt4) last_nt = (long long)(p - b) + 31 - __clz(nt4);
+            if (!t4) {
+                if (b4) badf |= 1u << min(field, 3u);
+                continue;
             }
-            bad1 = __any_sync(0xffffffffu, lb1);
-            bad2 = __any_sync(0xffffffffu, lb2);
-        }
-        if (lane == 0) {
-            uint32_t code = 0;
-            long long rid = 0;
-            LineRec lr;
-            lr.read_id = 0;
-            lr.s0 = b + f1b;
-            lr.l0 = 0;
-            lr.s1 = b + f2b;
-            lr.l1 = 0;
-            uint8_t fl = 0;
-            if (nf != 2 && nf != 3) {
-                code = 2;  // GX_EINVAL_LINE
-            } else if (!java_parse_long(text + b, tab[0], rid)) {
-                code = 3;  // GX_EINVAL_NUMBER
-            } else {
-                lr.read_id = rid;
-                lr.l0 = f1e - f1b;
-                if (nf == 3) {
-                    lr.l1 = f2e - f2b;
-                    fl |= LF_HAS_M1;
-                }
-                const bool id_ok = rid >= 0 && rid < (1LL << 35);
-                const bool m0v = lr.l0 > 0 && !bad1;
-                const bool m1v = nf == 3 && lr.l1 > 0 && !bad2;
-                if (m0v) {
-                    fl |= LF_M0_VALID;
-                    if (!id_ok)
-                        code = 4;  // GX_EREADID_RANGE
-                    else if ((uint32_t)k >= lr.l0)
-                        code = 5;  // GX_EREAD_TOO_SHORT
-                }
-                if (code == 0 && m1v) {
-                    fl |= LF_M1_VALID;
-                    if (!id_ok)
-                        code = 4;
-                    else if ((uint32_t)k >= lr.l1)
-                        code = 5;
+            for (uint32_t j = 0; j < 4; j++) {
+                if (!((vm >> j) & 1u)) continue;
+                if ((t4 >> j) & 1u) {
+                    const uint32_t at = (uint32_t)(p + j - b);
+                    if (tabs == 0)
+                        t0 = at;
+                    else if (tabs == 1)
+                        t1 = at;
+                    else if (tabs == 2)
+                        t2 = at;
+                    tabs++;
+                    field++;
+                } else if ((b4 >> j) & 1u) {
+                    badf |= 1u << min(field, 3u);
                 }
             }
-            if (code) {
-                atomicMin(&st->parse_err, ((unsigned long long)line << 8) | code);
-                fl = 0;
-            }
-            lines[line] = lr;
-            lflags[line] = fl;
-            nvalid[line] = (fl & LF_M0_VALID ? 1u : 0u) + (fl & LF_M1_VALID ? 1u : 0u);
         }
     }
+    // String.split: trailing empty fields removed; no tab at all gives one field
+    int nf;
+    if (tabs == 0)
+        nf = 1;
+    else if (last_nt < 0)
+        nf = 0;
+    else
+        nf = 1 + (int)tabs - (int)(len - 1 - (uint32_t)last_nt);
+    // field ranges (relative to b)
+    const uint32_t f1b = t0 + 1, f1e = tabs >= 2 ? t1 : len;
+    const uint32_t f2b = t1 + 1, f2e = tabs >= 3 ? t2 : len;
+    const bool bad1 = (badf >> 1) & 1u, bad2 = (badf >> 2) & 1u;
+    uint32_t code = 0;
+    long long rid = 0;
+    LineRec lr;
+    lr.read_id = 0;
+    lr.s0 = b + f1b;
+    lr.l0 = 0;
+    lr.s1 = b + f2b;
+    lr.l1 = 0;
+    uint8_t fl = 0;
+    if (nf != 2 && nf != 3) {
+        code = 2;  // GX_EINVAL_LINE
+    } else if (!java_parse_long(text + b, t0, rid)) {
+        code = 3;  // GX_EINVAL_NUMBER
+    } else {
+        lr.read_id = rid;
+        lr.l0 = f1e - f1b;
+        if (nf == 3) {
+            lr.l1 = f2e - f2b;
+            fl |= LF_HAS_M1;
+        }
+        const bool id_ok = rid >= 0 && rid < (1LL << 35);
+        const bool m0v = lr.l0 > 0 && !bad1;
+        const bool m1v = nf == 3 && lr.l1 > 0 && !bad2;
+        if (m0v) {
+            fl |= LF_M0_VALID;
+            if (!id_ok)
+                code = 4;  // GX_EREADID_RANGE
+            else if ((uint32_t)k >= lr.l0)
+                code = 5;  // GX_EREAD_TOO_SHORT
+        }
+        if (code == 0 && m1v) {
+            fl |= LF_M1_VALID;
+            if (!id_ok)
+                code = 4;
+            else if ((uint32_t)k >= lr.l1)
+                code = 5;
+        }
+    }
+    if (code) {
+        atomicMin(&st->parse_err, (line << 8) | code);
+        fl = 0;
+    }
+    lines[line] = lr;
+    lflags[line] = fl;
+    nvalid[line] = (fl & LF_M0_VALID ? 1u : 0u) + (fl & LF_M1_VALID ? 1u : 0u);
 }
 
 void launch_parse_lines(const uint8_t *text, uint64_t n_text, const unsigned long long *line_end, uint32_t n_lines,
                         int k, LineRec *lines, uint8_t *lflags, uint32_t *nvalid, DevStatus *st, cudaStream_t s) {
     if (!n_lines) return;
-    const uint64_t warps = n_lines;
-    uint64_t blocks = (warps * 32 + 255) / 256;
-    if (blocks > 0x7fffffffULL) blocks = 0x7fffffffULL;
     t_launches++;
-    k_parse_lines<<<(unsigned)blocks, 256, 0, s>>>(text, n_text, line_end, n_lines, k, lines, lflags, nvalid, st);
+    k_parse_lines<<<(n_lines + 255) / 256, 256, 0, s>>>(text, n_text, line_end, n_lines, k, lines, lflags, nvalid,
+                                                        st);
 }
 
 // list of valid reads (line << 1 | mate) and the occurrence count
@@ -2015,23 +1972,45 @@ template <> struct AggTable<u128> {
     }
 };
 
+// One fine bucket per CTA.  The bucket's distinct k-mers are counted in a shared-memory
+// open-addressing table (linear probing), then put in a deterministic order without sorting:
+// with linear probing the set of occupied slots, and the set of keys in each cluster (maximal
+// run of occupied slots), depend only on the keys, not on the order of the inserts.  So nodes
+// are numbered cluster by cluster, starting after the first empty slot, and by key inside a
+// cluster (a cluster that wraps past the last slot is numbered last).  Five phases with a
+// barrier between them:
+//   1. read heads (which claim or find their k-mer's slot and mark the set they belong to)
+//      and occurrences inserted: count += 1, edge bits OR-ed in only when new;
+//   2. occupancy bitmap (warp ballots) and per-warp counts;
+//   3. every node's rank: its cluster's start, the occupied slots before it, its place by key
+//      in the cluster; key, count/meta word and base record size out;
+//   4. warp 0 sorts, de-duplicates and sizes the read heads (at most 32: registers and
+//      shuffles) while warps 1-7 scan the base record sizes;
+//   5. record offsets (base offset + bytes of the kept heads of earlier nodes) and the read
+//      heads' output entries.
+// A bucket with more than 32 read heads sorts them with the whole block after phase 3 and
+// scans sizes that include them (the general path, rare).
 template <class K>
 struct AggSmem {
-    K key1[AGG_SLOTS];
-    uint32_t cnt[AGG_SLOTS];
-    uint32_t meta[AGG_SLOTS];
-    uint32_t nbytes[AGG_SLOTS];   // keys per home while ordering; then record bytes per node, then offsets
-    uint16_t ord[AGG_SLOTS];
+    K key1[AGG_SLOTS];                 // key + 1; 0 = empty
+    unsigned long long cm[AGG_SLOTS];  // count | meta << 32 (edge bits, read-head set flags)
+    uint32_t nbytes[AGG_SLOTS];        // record bytes per node in rank order, then offsets
+    uint16_t ord[AGG_SLOTS];           // slot of the node of each rank
     uint16_t rank_of_slot[AGG_SLOTS];
-    uint16_t home[AGG_SLOTS];     // home slot of each occupied slot's key
+    uint32_t occ[AGG_SLOTS / 32];      // occupancy bitmap
+    uint32_t wtot[8];                  // occupied slots in each warp's 256 slots
+    uint32_t ws7[8];                   // warps 1-7's scan
     unsigned long long ws[33];
-    unsigned long long wsk[32];   // warp 0's head sort
+    unsigned long long wsk[32];        // warp 0's head sort
     uint32_t wsv[32];
+    uint32_t hrank[32];                // kept read heads in order: their node's rank ...
+    uint32_t hcum[33];                 // ... and the bytes of the kept heads before each
     unsigned long long carry;
-    uint32_t n, fail, kept;
+    uint32_t n, fail, kept, base_total;
 };
 
 constexpr int AGG_BATCH = 8;  // occurrence loads in flight per thread
+static_assert(AGG_SLOTS == 2048, "k_aggregate maps 8 warps x 8 ballots onto the table");
 
 // first of the kept head keys (sorted) that is >= x
 __device__ __forceinline__ uint32_t kept_lower_bound(const unsigned long long *hk, uint32_t kept,
@@ -2047,18 +2026,74 @@ __device__ __forceinline__ uint32_t kept_lower_bound(const unsigned long long *h
     return lo;
 }
 
+__device__ __forceinline__ void bar_named(int id, int threads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+// Exclusive scan of v[0..n) in place by the 224 threads of warps 1-7 (named barrier 1);
+// returns the total.
+__device__ __forceinline__ uint32_t scan_warps_1_7(uint32_t *v, uint32_t n, uint32_t *ws7) {
+    const uint32_t t = threadIdx.x - 32;
+    const uint32_t per = (n + 223) / 224;
+    const uint32_t t0 = min(n, t * per), t1 = min(n, t0 + per);
+    uint32_t s = 0;
+    for (uint32_t j = t0; j < t1; j++) s += v[j];
+    const uint32_t inc = warp_inclusive_scan(s);
+    const int lane = threadIdx.x & 31, w = (int)(threadIdx.x >> 5) - 1;
+    if (lane == 31) ws7[w] = inc;
+    bar_named(1, 224);
+    uint32_t base = 0, total = 0;
+#pragma unroll
+    for (int i = 0; i < 7; i++) {
+        const uint32_t x = ws7[i];
+        if (i < w) base += x;
+        total += x;
+    }
+    uint32_t run = base + inc - s;
+    for (uint32_t j = t0; j < t1; j++) {
+        const uint32_t b = v[j];
+        v[j] = run;
+        run += b;
+    }
+    return total;
+}
+
+// the slot after the last empty slot before `slot` (cyclically); the table has an empty slot
+__device__ __forceinline__ uint32_t cluster_start(const uint32_t *occ, uint32_t slot) {
+    uint32_t wi = slot >> 5;
+    uint32_t m = ~occ[wi] & ((1u << (slot & 31)) - 1u);
+    while (!m) {
+        wi = (wi - 1) & (AGG_SLOTS / 32 - 1);
+        m = ~occ[wi];
+    }
+    return ((wi << 5) + (31 - __clz(m)) + 1) & (AGG_SLOTS - 1);
+}
+
+// bytes of a node's edge lists
+__device__ __forceinline__ uint32_t edge_bytes(uint32_t meta, int nb) {
+    uint32_t edges = 0;
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        const uint32_t m = (meta >> (4 * t)) & 15u;
+        if (m) edges += 4 + __popc(m) * (4 + nb);
+    }
+    return edges;
+}
+
 template <class K>
 __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggArgs a) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     AggSmem<K> &sm = *reinterpret_cast<AggSmem<K> *>(smem_raw);
+    const unsigned full = 0xffffffffu;
     const uint32_t f = blockIdx.x;
     const int nb = (a.k + 3) / 4;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned long long o0 = a.fine_off[f], o1 = a.fine_off[f + 1];
     const K *okey = (const K *)a.okey2 + o0;
     const uint16_t *obits = a.obits2 + o0;
     const uint32_t M = (uint32_t)(o1 - o0);
     // A bucket with at most 32 read heads (the usual case) leaves them to warp 0: lane i loads
-    // head i's entry, its read and the read's line now, so the loads land while the table fills.
+    // head i's entry, its read and the read's line now, so the loads land while the table clears.
     const uint32_t hb = a.head_off[f], hc = a.head_cnt[f];
     const bool warp_heads = hc <= 32;
     uint32_t p_r = 0xffffffffu, p_rl = 0;
@@ -2070,9 +2105,6 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         p_rl = a.reads[p_r];
         p_lr = a.lines[p_rl >> 1];
     }
-    // 1. aggregate the bucket's occurrences: count += 1, edge mask |= bits; each thread
-    //    loads AGG_BATCH occurrences before inserting any of them (the first batch's loads go
-    //    out before the table is cleared)
     K kk[AGG_BATCH];
     uint32_t bb[AGG_BATCH];
 #pragma unroll
@@ -2085,17 +2117,48 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         const uint4 z = make_uint4(0, 0, 0, 0);
         uint4 *k4 = reinterpret_cast<uint4 *>(sm.key1);
         for (uint32_t i = threadIdx.x; i < AGG_SLOTS * sizeof(K) / 16; i += blockDim.x) k4[i] = z;
-        for (uint32_t i = threadIdx.x; i < AGG_SLOTS / 4; i += blockDim.x) {
-            reinterpret_cast<uint4 *>(sm.cnt)[i] = z;
-            reinterpret_cast<uint4 *>(sm.meta)[i] = z;
-            reinterpret_cast<uint4 *>(sm.nbytes)[i] = z;
-        }
+        uint4 *c4 = reinterpret_cast<uint4 *>(sm.cm);
+        for (uint32_t i = threadIdx.x; i < AGG_SLOTS / 2; i += blockDim.x) c4[i] = z;
     }
     if (threadIdx.x == 0) {
         sm.n = 0;
         sm.fail = 0;
     }
     __syncthreads();
+    // ---- 1. read heads, then occurrences ----
+    // A head claims (or finds) its first k-mer's slot and marks the set it belongs to; that
+    // k-mer is one of the bucket's occurrences, which give the count.
+    if (warp_heads) {
+        if (threadIdx.x < hc) {
+            const K key = (K)(((u128)p_h.khi << 64) | p_h.klo);
+            uint32_t claimed = 0;
+            const int sl = AggTable<K>::insert(sm.key1, key, (uint32_t)KeyOps<K>::hash(key), claimed);
+            if (sl < 0) {
+                sm.fail = 1;
+                p_h.slot = 0;
+            } else {
+                if (claimed) atomicAdd(&sm.n, 1u);
+                atomicOr(&sm.cm[sl], (unsigned long long)((p_h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED)
+                                         << 32);
+                p_h.slot = (uint32_t)sl;
+            }
+        }
+    } else {
+        for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
+            const uint32_t r = a.head_idx[hb + i];
+            const Head h = a.heads[r];
+            const K key = (K)(((u128)h.khi << 64) | h.klo);
+            uint32_t claimed = 0;
+            const int sl = AggTable<K>::insert(sm.key1, key, (uint32_t)KeyOps<K>::hash(key), claimed);
+            if (sl < 0) {
+                sm.fail = 1;
+                continue;
+            }
+            if (claimed) atomicAdd(&sm.n, 1u);
+            atomicOr(&sm.cm[sl], (unsigned long long)((h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED) << 32);
+            a.heads[r].slot = (uint32_t)sl;
+        }
+    }
     for (uint32_t c0 = 0; c0 < M; c0 += AGG_BATCH * blockDim.x) {
         if (c0) {
 #pragma unroll
@@ -2110,110 +2173,95 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
             if (i >= M) continue;
             uint32_t claimed = 0;
-            const uint32_t h = (uint32_t)KeyOps<K>::hash(kk[q]);
-            const int sl = AggTable<K>::insert(sm.key1, kk[q], h, claimed);
+            const int sl = AggTable<K>::insert(sm.key1, kk[q], (uint32_t)KeyOps<K>::hash(kk[q]), claimed);
             if (sl < 0) {
                 sm.fail = 1;
                 continue;
             }
-            if (claimed) {
-                atomicAdd(&sm.n, 1u);
-                sm.home[sl] = (uint16_t)(h & (AGG_SLOTS - 1));  // where its probe started
-            }
-            atomicAdd(&sm.cnt[sl], 1u);
-            if (bb[q]) atomicOr(&sm.meta[sl], bb[q]);
+            if (claimed) atomicAdd(&sm.n, 1u);
+            const unsigned long long old = atomicAdd(&sm.cm[sl], 1ULL);
+            if (bb[q] & ~(uint32_t)(old >> 32)) atomicOr(&sm.cm[sl], (unsigned long long)bb[q] << 32);
         }
     }
     __syncthreads();
-    if (sm.fail) {
+    const uint32_t n = sm.n;
+    if (sm.fail || n >= AGG_SLOTS) {  // the ordering below needs an empty slot
         if (threadIdx.x == 0) atomicAdd(&a.st->table_full, 1u);
         return;
     }
-    // 2. read heads: find their node, mark the unflipped / flipped set
-    if (warp_heads) {
-        if (threadIdx.x < hc) {
-            const K key = (K)(((u128)p_h.khi << 64) | p_h.klo);
-            const int sl = AggTable<K>::find(sm.key1, key, (uint32_t)KeyOps<K>::hash(key));
-            if (sl < 0) {
-                atomicAdd(&a.st->internal_err, 1u);
-                p_h.slot = 0;
-            } else {
-                atomicOr(&sm.meta[sl], (p_h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
-                p_h.slot = (uint32_t)sl;
-            }
-        }
-    } else {
-        for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
-            const uint32_t r = a.head_idx[hb + i];
-            Head h = a.heads[r];
-            const K key = (K)(((u128)h.khi << 64) | h.klo);
-            const int sl = AggTable<K>::find(sm.key1, key, (uint32_t)KeyOps<K>::hash(key));
-            if (sl < 0) {
-                atomicAdd(&a.st->internal_err, 1u);
-                continue;
-            }
-            atomicOr(&sm.meta[sl], (h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
-            h.slot = (uint32_t)sl;
-            a.heads[r] = h;
-        }
+    // ---- 2. occupancy: warp w owns slots [256 w, 256 w + 256), lane q keeps word 8 w + q ----
+    uint32_t myocc = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const uint32_t b = __ballot_sync(full, sm.key1[warp * 256 + q * 32 + lane] != (K)0);
+        if (lane == q) myocc = b;
     }
-    // 3. order the nodes deterministically: by home slot (the low hash bits that started the
-    //    probe), then by key.  A counting sort over the 2048 homes: keys per home (nbytes),
-    //    their offsets, then each key's place among the keys of its home, counted back along
-    //    its probe run (the keys of one home all lie between the home and the key's slot).
-    //    (The counts only read the finished table, like the head lookups above: no barrier
-    //    between them.)
-    for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x)
-        if (sm.key1[i] != (K)0) atomicAdd(&sm.nbytes[sm.home[i]], 1u);
+    const uint32_t pc = lane < 8 ? __popc(myocc) : 0u;
+    const uint32_t pc_incl = warp_inclusive_scan(pc);
+    if (lane < 8) sm.occ[warp * 8 + lane] = myocc;
+    if (lane == 7) sm.wtot[warp] = pc_incl;
     __syncthreads();
-    const uint32_t n_keys = block_scan_array(sm.nbytes, AGG_SLOTS, reinterpret_cast<uint32_t *>(sm.ws));
-    for (uint32_t i = threadIdx.x; i < AGG_SLOTS; i += blockDim.x) {
-        if (sm.key1[i] == (K)0) continue;
-        const uint32_t hm = sm.home[i];
-        uint32_t before = 0;
-        for (uint32_t j = hm; j != i; j = (j + 1) & (AGG_SLOTS - 1))
-            if (sm.key1[j] != (K)0 && sm.home[j] == hm) before++;
-        sm.ord[sm.nbytes[hm] + before] = (uint16_t)i;
+    // ---- 3. ranks ----
+    // When a cluster wraps from the last slot to the first, its part at the front (the slots
+    // before the first empty one, z) is numbered last: ranks start z slots in.
+    uint32_t z = 0;
+    if (sm.occ[AGG_SLOTS / 32 - 1] >> 31) {
+        const uint32_t w0 = sm.occ[lane], w1 = sm.occ[lane + 32];
+        const uint32_t nf0 = __ballot_sync(full, w0 != full), nf1 = __ballot_sync(full, w1 != full);
+        const uint32_t zw = nf0 ? (uint32_t)__ffs(nf0) - 1 : 32u + (uint32_t)__ffs(nf1) - 1;
+        const uint32_t zword = __shfl_sync(full, zw < 32 ? w0 : w1, (int)(zw & 31));
+        z = zw * 32 + (uint32_t)__ffs(~zword) - 1;
     }
-    __syncthreads();
-    for (uint32_t hm = threadIdx.x; hm < AGG_SLOTS; hm += blockDim.x) {
-        const uint32_t b0 = sm.nbytes[hm], c = (hm + 1 < AGG_SLOTS ? sm.nbytes[hm + 1] : n_keys) - b0;
-        for (uint32_t u = 1; u < c; u++)
-            for (uint32_t v = b0 + u; v > b0 && sm.key1[sm.ord[v]] < sm.key1[sm.ord[v - 1]]; v--) {
-                const uint16_t t = sm.ord[v];
-                sm.ord[v] = sm.ord[v - 1];
-                sm.ord[v - 1] = t;
-            }
-    }
-    const uint32_t n = sm.n;
-    __syncthreads();
-    // 4. nodes out (over the bucket's own occurrence range); record bytes without heads
+    const uint32_t wbase = __reduce_add_sync(full, lane < warp ? sm.wtot[lane] : 0u);
     K *nkey = (K *)a.nkey + o0;
     unsigned long long *ncm = a.ncm + o0;
-    uint32_t inexact = 0;
-    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-        const uint32_t o = sm.ord[j];
-        sm.rank_of_slot[o] = (uint16_t)j;
-        nkey[j] = sm.key1[o] - 1;
-        ncm[j] = (unsigned long long)sm.cnt[o] | ((unsigned long long)sm.meta[o] << 32);
-        if (sm.cnt[o] >= (1u << 24)) inexact++;
-        sm.nbytes[j] = node_base_bytes(sm.meta[o], nb);
+    uint32_t inexact = 0, phantom = 0;
+#pragma unroll 2
+    for (int q = 0; q < 8; q++) {
+        const uint32_t word = __shfl_sync(full, myocc, q);
+        const uint32_t wpre = __shfl_sync(full, pc_incl - pc, q);
+        const uint32_t slot = warp * 256 + q * 32 + lane;
+        if (!((word >> lane) & 1u)) continue;
+        const uint32_t before = wbase + wpre + __popc(word & ((1u << lane) - 1u));  // occupied slots before
+        const uint32_t c0 = cluster_start(sm.occ, slot);
+        // occupied slots before the cluster: the run from c0 to this slot is all occupied; a
+        // cluster that wraps past the last slot occupies everything from c0 to the end
+        const uint32_t pre_c0 = c0 <= slot ? before - (slot - c0) : n - (AGG_SLOTS - c0);
+        const K mine = sm.key1[slot];
+        uint32_t within = 0;
+        for (uint32_t j = c0;; j = (j + 1) & (AGG_SLOTS - 1)) {
+            if (!((sm.occ[j >> 5] >> (j & 31)) & 1u)) break;
+            within += sm.key1[j] < mine ? 1u : 0u;
+        }
+        const uint32_t rank = pre_c0 - z + within;
+        if (rank >= n) {  // never expected: the ranks are a permutation of [0, n)
+            phantom++;
+            continue;
+        }
+        sm.rank_of_slot[slot] = (uint16_t)rank;
+        sm.ord[rank] = (uint16_t)slot;
+        const unsigned long long cmv = sm.cm[slot];
+        nkey[rank] = mine - 1;
+        ncm[rank] = cmv;
+        const uint32_t cnt = (uint32_t)cmv;
+        if (cnt >= (1u << 24)) inexact++;
+        if (cnt == 0) phantom++;  // a read head whose k-mer has no occurrence here
+        sm.nbytes[rank] = node_base_bytes((uint32_t)(cmv >> 32), nb);
     }
     if (inexact) atomicAdd(&a.st->cov_inexact, inexact);
+    if (phantom) atomicAdd(&a.st->internal_err, phantom);
     __syncthreads();
-    // 5. read heads: sort by (node, TreeSet order), keep the first of equal uuids.  A bucket
-    //    with at most 32 heads (the usual case) leaves them to warp 0, in registers; larger
-    //    ones sort in global scratch with the whole block.
-    unsigned long long *hk = a.head_sk + hb;
-    uint32_t *hv = a.head_idx + hb;
-    const int lane = threadIdx.x & 31;
-    unsigned long long wk = 0;  // warp path: this lane's head in sorted order, kept or not
-    uint32_t wkeep = 0, wkept_idx = 0, wkeep_mask = 0;
-    // warp path: the sorted head's uuid, sequence offsets and lengths (from the lane that loaded it)
-    unsigned long long w_uuid = 0, w_soff = 0, w_moff = 0;
-    uint32_t w_L = 0, w_Lm = 0;
+    HeadOut *hout = a.hout + hb;
+    const uint32_t keylen = 4 + nb;
+    uint32_t *noff = a.noff + o0;
     if (warp_heads) {
-        if (threadIdx.x < 32) {
+        // ---- 4. warp 0: read heads sorted by (node, TreeSet order), duplicates dropped;
+        //         warps 1-7: exclusive scan of the base record sizes ----
+        unsigned long long wk = 0;
+        uint32_t wkeep = 0, wkept_idx = 0, wkeep_mask = 0, hsz = 0, w_slot = 0;
+        unsigned long long w_uuid = 0, w_soff = 0, w_moff = 0;
+        uint32_t w_L = 0, w_Lm = 0;
+        if (warp == 0) {
             unsigned long long mk = ~0ULL;
             uint32_t mv = 0xffffffffu;
             if (lane < (int)hc) {
@@ -2222,8 +2270,8 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             }
             uint32_t rank = 0;
             for (int j = 0; j < (int)hc; j++) {
-                const unsigned long long kj = __shfl_sync(0xffffffffu, mk, j);
-                const uint32_t vj = __shfl_sync(0xffffffffu, mv, j);
+                const unsigned long long kj = shfl64(mk, j);
+                const uint32_t vj = __shfl_sync(full, mv, j);
                 rank += (kj < mk || (kj == mk && vj < mv)) ? 1u : 0u;
             }
             if (lane < (int)hc) {
@@ -2240,122 +2288,50 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             w_uuid = shfl64(p_h.uuid, (int)src);
             w_soff = shfl64(mate ? p_lr.s1 : p_lr.s0, (int)src);
             w_moff = shfl64(mate ? p_lr.s0 : p_lr.s1, (int)src);
-            w_L = __shfl_sync(0xffffffffu, mate ? p_lr.l1 : p_lr.l0, (int)src);
-            w_Lm = __shfl_sync(0xffffffffu, mate ? p_lr.l0 : p_lr.l1, (int)src);
-            const unsigned long long prev = __shfl_up_sync(0xffffffffu, wk, 1);
+            w_L = __shfl_sync(full, mate ? p_lr.l1 : p_lr.l0, (int)src);
+            w_Lm = __shfl_sync(full, mate ? p_lr.l0 : p_lr.l1, (int)src);
+            w_slot = __shfl_sync(full, p_h.slot, (int)src);
+            const unsigned long long prev = shfl64(wk, lane > 0 ? lane - 1 : 0);
             wkeep = (lane < (int)hc && (lane == 0 || wk != prev)) ? 1u : 0u;
-            wkeep_mask = __ballot_sync(0xffffffffu, wkeep);
+            wkeep_mask = __ballot_sync(full, wkeep);
             wkept_idx = __popc(wkeep_mask & ((1u << lane) - 1u));
-            if (wkeep)
-                atomicAdd(&sm.nbytes[(uint32_t)(wk >> 37)],
-                          1 + 8 + 4 + packed_len(w_L) + (w_Lm > 0 ? 4 + packed_len(w_Lm) : 0));
-            if (lane == 0) sm.kept = __popc(wkeep_mask);
-        }
-        __syncthreads();
-    } else {
-        if (hc > HEAD_CAP && threadIdx.x == 0) atomicAdd(&a.st->big_head_parts, 1u);
-        for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
-            const uint32_t r = hv[i];
-            const Head h = a.heads[r];
-            hk[i] = head_sort_key(sm.rank_of_slot[h.slot], h.uuid);
-        }
-        __syncthreads();
-        if (hc <= blockDim.x) {
-            // few heads (the usual case): each thread places its own by counting the smaller
-            // (key, read) pairs; read ordinals are distinct, so the ranks are too
-            unsigned long long mk = 0;
-            uint32_t mv = 0, rank = 0;
-            if (threadIdx.x < hc) {
-                mk = hk[threadIdx.x];
-                mv = hv[threadIdx.x];
-                for (uint32_t j = 0; j < hc; j++) {
-                    const unsigned long long kj = hk[j];
-                    const uint32_t vj = hv[j];
-                    rank += (kj < mk || (kj == mk && vj < mv)) ? 1u : 0u;
-                }
+            hsz = wkeep ? 1 + 8 + 4 + packed_len(w_L) + (w_Lm > 0 ? 4 + packed_len(w_Lm) : 0) : 0u;
+            const uint32_t incl = warp_inclusive_scan(hsz);
+            const uint32_t kept_w = __popc(wkeep_mask);
+            // kept heads in order: node rank and the bytes of the kept heads before
+            if (wkeep) {
+                sm.hrank[wkept_idx] = (uint32_t)(wk >> 37);
+                sm.hcum[wkept_idx] = incl - hsz;
             }
-            __syncthreads();
-            if (threadIdx.x < hc) {
-                hk[rank] = mk;
-                hv[rank] = mv;
-            }
-            __syncthreads();
+            if (lane == 31) sm.hcum[kept_w] = incl;
+            if ((uint32_t)lane >= kept_w) sm.hrank[lane] = 0xffffffffu;  // padding for the search
+            if (lane == 0) sm.kept = kept_w;
         } else {
-            bitonic_sort_pairs<unsigned long long, uint32_t>(hk, hv, hc);
-        }
-        if (threadIdx.x == 0) {
-            sm.kept = 0;
-            sm.carry = 0;
+            const uint32_t t = scan_warps_1_7(sm.nbytes, n, sm.ws7);
+            if (threadIdx.x == 32) sm.base_total = t;
         }
         __syncthreads();
-        for (uint32_t c0 = 0; c0 < hc; c0 += blockDim.x) {
-            const uint32_t i = c0 + threadIdx.x;
-            unsigned long long key = 0;
-            uint32_t keep = 0, r = 0;
-            if (i < hc) {
-                key = hk[i];
-                const unsigned long long prev = i == 0 ? ~0ULL : (i == c0 ? sm.carry : hk[i - 1]);
-                keep = key != prev ? 1u : 0u;
-                r = hv[i];
-            }
-            const unsigned long long last = hk[min(hc, c0 + blockDim.x) - 1];
-            unsigned long long tot;
-            const unsigned long long ex = block_exclusive_scan((unsigned long long)keep, sm.ws, tot);
-            if (keep) {
-                const uint32_t w = sm.kept + (uint32_t)ex;
-                hk[w] = key;
-                hv[w] = r;
-                const uint32_t rank = (uint32_t)(key >> 37);
-                const uint32_t rl = a.reads[r];
-                atomicAdd(&sm.nbytes[rank], head_bytes(a.lines[rl >> 1], rl & 1u));
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                sm.kept += (uint32_t)tot;
-                sm.carry = last;
-            }
-            __syncthreads();
+        // ---- 5. record offsets; read-head entries ----
+        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+            // kept heads of nodes before j: hrank is sorted, padded with ~0 to 32 entries
+            uint32_t pos = 0;
+#pragma unroll
+            for (uint32_t step = 16; step > 0; step >>= 1)
+                if (sm.hrank[pos + step - 1] < j) pos += step;
+            if (sm.hrank[pos] < j) pos++;  // all 32 before j
+            noff[j] = sm.nbytes[j] + sm.hcum[pos];
         }
-    }
-    const uint32_t kept = sm.kept;
-    // 6. record offsets of the nodes in the partition
-    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
-    const uint32_t t0 = min(n, threadIdx.x * per), t1 = min(n, t0 + per);
-    unsigned long long mine = 0;
-    for (uint32_t j = t0; j < t1; j++) mine += sm.nbytes[j];
-    unsigned long long tot_bytes;
-    unsigned long long run = block_exclusive_scan(mine, sm.ws, tot_bytes);
-    uint32_t *noff = a.noff + o0;
-    for (uint32_t j = t0; j < t1; j++) {
-        const uint32_t b = sm.nbytes[j];
-        sm.nbytes[j] = (uint32_t)run;
-        noff[j] = (uint32_t)run;
-        run += b;
-    }
-    __syncthreads();
-    // 7. byte position of every kept head: node offset, frame + key + active + edges, the
-    //    set headers, the heads of the node before it
-    HeadOut *hout = a.hout + hb;
-    const uint32_t keylen = 4 + nb;
-    if (warp_heads) {
-        if (threadIdx.x < 32) {
-            const uint32_t hsz = wkeep ? 1 + 8 + 4 + packed_len(w_L) + (w_Lm > 0 ? 4 + packed_len(w_Lm) : 0) : 0u;
-            const uint32_t pre = warp_inclusive_scan(hsz) - hsz;  // bytes of the kept heads before
+        if (warp == 0) {
+            const uint32_t kept_w = __popc(wkeep_mask);
             const uint32_t rank = (uint32_t)(wk >> 37);
             const bool flipped = (wk >> 36) & 1ULL;
             // the node's kept lanes, its flipped ones, its first lane
-            const uint32_t node_mask = __match_any_sync(0xffffffffu, wkeep ? rank : 0xffffffffu) & wkeep_mask;
-            const uint32_t flip_mask = __ballot_sync(0xffffffffu, wkeep && flipped);
-            const int first = node_mask ? __ffs(node_mask) - 1 : 0;
-            const uint32_t pre0 = __shfl_sync(0xffffffffu, pre, first);
+            const uint32_t node_mask = __match_any_sync(full, wkeep ? rank : 0xffffffffu) & wkeep_mask;
+            const uint32_t flip_mask = __ballot_sync(full, wkeep && flipped);
             if (wkeep) {
+                const int first = __ffs(node_mask) - 1;
                 const uint32_t cu = __popc(node_mask & ~flip_mask), cf = __popc(node_mask & flip_mask);
-                const uint32_t meta = sm.meta[sm.ord[rank]];
-                uint32_t edges = 0;
-                for (int t = 0; t < 4; t++) {
-                    const uint32_t m = (meta >> (4 * t)) & 15u;
-                    if (m) edges += 4 + __popc(m) * (4 + nb);
-                }
+                const uint32_t meta = (uint32_t)(sm.cm[w_slot] >> 32);
                 const uint32_t st = __popc(wkeep_mask & ((1u << first) - 1u));  // kept index of the node's first
                 HeadOut ho;
                 ho.uuid = w_uuid;
@@ -2363,75 +2339,156 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
                 ho.m_off = w_moff;
                 ho.L = w_L;
                 ho.Lm = w_Lm;
-                ho.pos = sm.nbytes[rank] + 8 + keylen + 1 + edges + 5 + ((flipped && cu > 0) ? 5 : 0) + (pre - pre0);
+                ho.pos = sm.nbytes[rank] + sm.hcum[wkept_idx] + 8 + keylen + 1 + edge_bytes(meta, nb) + 5 +
+                         ((flipped && cu > 0) ? 5 : 0);
                 ho.set_count = (wkept_idx == st && !flipped) ? cu : ((flipped && wkept_idx == st + cu) ? cf : 0u);
                 ho.part = f;
                 hout[wkept_idx] = ho;
             }
             // the slots past the kept heads: duplicates, skipped by the head writer
-            const uint32_t kept_w = __popc(wkeep_mask);
             if ((uint32_t)lane >= kept_w && (uint32_t)lane < hc) hout[lane].part = HEAD_DROPPED;
         }
-    } else {
-        unsigned long long hrun = 0;
-        for (uint32_t c0 = 0; c0 < kept; c0 += blockDim.x) {
-            const uint32_t i = c0 + threadIdx.x;
-            uint32_t hsz = 0, r = 0, rl = 0;
-            LineRec lr{};
-            if (i < kept) {
-                r = hv[i];
-                rl = a.reads[r];
-                lr = a.lines[rl >> 1];
-                hsz = head_bytes(lr, rl & 1u);
+        if (threadIdx.x == 0) {
+            a.part_nodes[f] = n;
+            a.part_bytes[f] = (unsigned long long)sm.base_total + sm.hcum[sm.kept];
+            a.head_cnt2[f] = sm.kept;
+        }
+        return;
+    }
+    // ---- the general path: more than 32 read heads ----
+    unsigned long long *hk = a.head_sk + hb;
+    uint32_t *hv = a.head_idx + hb;
+    if (hc > HEAD_CAP && threadIdx.x == 0) atomicAdd(&a.st->big_head_parts, 1u);
+    for (uint32_t i = threadIdx.x; i < hc; i += blockDim.x) {
+        const uint32_t r = hv[i];
+        const Head h = a.heads[r];
+        hk[i] = head_sort_key(sm.rank_of_slot[h.slot], h.uuid);
+    }
+    __syncthreads();
+    if (hc <= blockDim.x) {
+        // each thread places its own head by counting the smaller (key, read) pairs; read
+        // ordinals are distinct, so the ranks are too
+        unsigned long long mk = 0;
+        uint32_t mv = 0, rank = 0;
+        if (threadIdx.x < hc) {
+            mk = hk[threadIdx.x];
+            mv = hv[threadIdx.x];
+            for (uint32_t j = 0; j < hc; j++) {
+                const unsigned long long kj = hk[j];
+                const uint32_t vj = hv[j];
+                rank += (kj < mk || (kj == mk && vj < mv)) ? 1u : 0u;
             }
-            unsigned long long tot;
-            const unsigned long long ex = block_exclusive_scan((unsigned long long)hsz, sm.ws, tot);
-            // the running byte count of kept heads: stash each head's prefix in hk's low bits
-            if (i < kept) {
-                const unsigned long long pre = hrun + ex;
-                const unsigned long long key = hk[i];
-                hk[i] = (key & ~((1ULL << 36) - 1)) | pre;  // rank << 37 | flipped << 36 | prefix
-            }
-            hrun += tot;
         }
         __syncthreads();
-        for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
-            const unsigned long long key = hk[i];
-            const uint32_t rank = (uint32_t)(key >> 37);
-            const bool flipped = (key >> 36) & 1ULL;
-            // the node's kept heads: [st, st + cu) unflipped, then cf flipped (hk is sorted by
-            // rank, flipped, position)
-            const unsigned long long rbase = (unsigned long long)rank << 37;
-            const uint32_t st = kept_lower_bound(hk, kept, rbase);
-            const uint32_t fl = kept_lower_bound(hk, kept, rbase | (1ULL << 36));
-            const uint32_t cu = fl - st, cf = kept_lower_bound(hk, kept, rbase + (1ULL << 37)) - fl;
-            const unsigned long long pre = key & ((1ULL << 36) - 1);
-            const unsigned long long pre0 = hk[st] & ((1ULL << 36) - 1);
-            const uint32_t meta = sm.meta[sm.ord[rank]];
-            uint32_t edges = 0;
-            for (int t = 0; t < 4; t++) {
-                const uint32_t m = (meta >> (4 * t)) & 15u;
-                if (m) edges += 4 + __popc(m) * (4 + nb);
-            }
-            const uint32_t pos = sm.nbytes[rank] + 8 + keylen + 1 + edges + 5 + ((flipped && cu > 0) ? 5 : 0) +
-                                 (uint32_t)(pre - pre0);
-            const uint32_t r = hv[i];
-            const uint32_t rl = a.reads[r];
-            const LineRec lr = a.lines[rl >> 1];
-            const uint32_t mate = rl & 1u;
-            HeadOut ho;
-            ho.uuid = a.heads[r].uuid;
-            ho.s_off = mate ? lr.s1 : lr.s0;
-            ho.m_off = mate ? lr.s0 : lr.s1;
-            ho.L = mate ? lr.l1 : lr.l0;
-            ho.Lm = mate ? lr.l0 : lr.l1;
-            ho.pos = pos;
-            ho.set_count = (i == st && !flipped) ? cu : ((flipped && i == st + cu) ? cf : 0u);
-            ho.part = f;
-            hout[i] = ho;
+        if (threadIdx.x < hc) {
+            hk[rank] = mk;
+            hv[rank] = mv;
         }
-        for (uint32_t i = kept + threadIdx.x; i < hc; i += blockDim.x) hout[i].part = HEAD_DROPPED;
+        __syncthreads();
+    } else {
+        bitonic_sort_pairs<unsigned long long, uint32_t>(hk, hv, hc);
     }
+    if (threadIdx.x == 0) {
+        sm.kept = 0;
+        sm.carry = 0;
+    }
+    __syncthreads();
+    // keep the first of equal keys; add the kept heads' bytes to their node's size
+    for (uint32_t c0 = 0; c0 < hc; c0 += blockDim.x) {
+        const uint32_t i = c0 + threadIdx.x;
+        unsigned long long key = 0;
+        uint32_t keep = 0, r = 0;
+        if (i < hc) {
+            key = hk[i];
+            const unsigned long long prev = i == 0 ? ~0ULL : (i == c0 ? sm.carry : hk[i - 1]);
+            keep = key != prev ? 1u : 0u;
+            r = hv[i];
+        }
+        const unsigned long long last = hk[min(hc, c0 + blockDim.x) - 1];
+        unsigned long long tot;
+        const unsigned long long ex = block_exclusive_scan((unsigned long long)keep, sm.ws, tot);
+        if (keep) {
+            const uint32_t w = sm.kept + (uint32_t)ex;
+            hk[w] = key;
+            hv[w] = r;
+            const uint32_t rank = (uint32_t)(key >> 37);
+            const uint32_t rl = a.reads[r];
+            atomicAdd(&sm.nbytes[rank], head_bytes(a.lines[rl >> 1], rl & 1u));
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            sm.kept += (uint32_t)tot;
+            sm.carry = last;
+        }
+        __syncthreads();
+    }
+    const uint32_t kept = sm.kept;
+    // record offsets of the nodes, read heads included
+    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t t0 = min(n, threadIdx.x * per), t1 = min(n, t0 + per);
+    unsigned long long mine = 0;
+    for (uint32_t j = t0; j < t1; j++) mine += sm.nbytes[j];
+    unsigned long long tot_bytes;
+    unsigned long long run = block_exclusive_scan(mine, sm.ws, tot_bytes);
+    for (uint32_t j = t0; j < t1; j++) {
+        const uint32_t b = sm.nbytes[j];
+        sm.nbytes[j] = (uint32_t)run;
+        noff[j] = (uint32_t)run;
+        run += b;
+    }
+    __syncthreads();
+    // byte position of every kept head: node offset, frame + key + active + edges, the set
+    // headers, the heads of the node before it
+    unsigned long long hrun = 0;
+    for (uint32_t c0 = 0; c0 < kept; c0 += blockDim.x) {
+        const uint32_t i = c0 + threadIdx.x;
+        uint32_t hsz = 0;
+        if (i < kept) {
+            const uint32_t rl = a.reads[hv[i]];
+            hsz = head_bytes(a.lines[rl >> 1], rl & 1u);
+        }
+        unsigned long long tot;
+        const unsigned long long ex = block_exclusive_scan((unsigned long long)hsz, sm.ws, tot);
+        // the running byte count of kept heads: stash each head's prefix in hk's low bits
+        if (i < kept) {
+            const unsigned long long pre = hrun + ex;
+            const unsigned long long key = hk[i];
+            hk[i] = (key & ~((1ULL << 36) - 1)) | pre;  // rank << 37 | flipped << 36 | prefix
+        }
+        hrun += tot;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
+        const unsigned long long key = hk[i];
+        const uint32_t rank = (uint32_t)(key >> 37);
+        const bool flipped = (key >> 36) & 1ULL;
+        // the node's kept heads: [st, st + cu) unflipped, then cf flipped (hk is sorted by
+        // rank, flipped, position)
+        const unsigned long long rbase = (unsigned long long)rank << 37;
+        const uint32_t st = kept_lower_bound(hk, kept, rbase);
+        const uint32_t fl = kept_lower_bound(hk, kept, rbase | (1ULL << 36));
+        const uint32_t cu = fl - st, cf = kept_lower_bound(hk, kept, rbase + (1ULL << 37)) - fl;
+        const unsigned long long pre = key & ((1ULL << 36) - 1);
+        const unsigned long long pre0 = hk[st] & ((1ULL << 36) - 1);
+        const uint32_t meta = (uint32_t)(sm.cm[sm.ord[rank]] >> 32);
+        const uint32_t pos = sm.nbytes[rank] + 8 + keylen + 1 + edge_bytes(meta, nb) + 5 +
+                             ((flipped && cu > 0) ? 5 : 0) + (uint32_t)(pre - pre0);
+        const uint32_t r = hv[i];
+        const uint32_t rl = a.reads[r];
+        const LineRec lr = a.lines[rl >> 1];
+        const uint32_t mate = rl & 1u;
+        HeadOut ho;
+        ho.uuid = a.heads[r].uuid;
+        ho.s_off = mate ? lr.s1 : lr.s0;
+        ho.m_off = mate ? lr.s0 : lr.s1;
+        ho.L = mate ? lr.l1 : lr.l0;
+        ho.Lm = mate ? lr.l0 : lr.l1;
+        ho.pos = pos;
+        ho.set_count = (i == st && !flipped) ? cu : ((flipped && i == st + cu) ? cf : 0u);
+        ho.part = f;
+        hout[i] = ho;
+    }
+    for (uint32_t i = kept + threadIdx.x; i < hc; i += blockDim.x) hout[i].part = HEAD_DROPPED;
     if (threadIdx.x == 0) {
         a.part_nodes[f] = n;
         a.part_bytes[f] = tot_bytes;

@@ -148,6 +148,9 @@ typedef struct gx_stats {
     uint64_t attempts;        /* passes run: 1, plus one per table/bucket overflow retried */
     double ms_layout;         /* device time of the regrouping into the reference's parts
                                  (GX_LAYOUT_REFERENCE_PARTS; 0 otherwise) */
+    uint64_t super_counted;   /* partitioned build: 1 when it counted its super buckets before
+                                 scattering (a hot bucket, or room per bucket beyond the memory
+                                 limit), 0 when it scattered straight away */
 } gx_stats;
 
 /* ---- context ------------------------------------------------------------------------- */
