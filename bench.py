@@ -538,30 +538,45 @@ def run_gb300(args, ws, rank, local):
     out_bytes = stats[0]["record_bytes"]
     outs = [gx.PinnedBuffer(out_bytes + 16), gx.PinnedBuffer(out_bytes + 16)]
 
-    def run_e2e(n):
+    def run_e2e(n, stamps=None):
         """n jobs back to back, each: pinned text in, build, every record out into pinned memory.
         Job i's copy out (asynchronous emit) overlaps job i + 1's copy in and build; the two
-        output buffers alternate."""
+        output buffers alternate.  `stamps` collects, per job, the host time of each call and
+        the build's device time."""
         prev = None
         for i in range(n):
+            t0 = time.perf_counter()
             job = gx.GraphBuildJob(ctx, w.k, **pin)
             job.add_input(pin_in)
+            t1 = time.perf_counter()
             job.run()
+            t2 = time.perf_counter()
             wr, more = job.emit_async(0, outs[i % 2].ptr, outs[i % 2].nbytes)
             assert not more and wr == out_bytes
+            t3 = time.perf_counter()
             if prev is not None:
                 prev.emit_wait()
+                t4 = time.perf_counter()
                 prev.close()
+            else:
+                t4 = t3
+            t5 = time.perf_counter()
+            if stamps is not None:
+                stamps.append((t1 - t0, t2 - t1, t3 - t2, t4 - t3, t5 - t4, job.stats()["ms_total"]))
             prev = job
         prev.emit_wait()
         prev.close()
 
     run_e2e(max(2, args.warmup // 2))
     barrier(ws)
+    stamps = []
     ctx.mark(2)
-    run_e2e(args.steps)
+    run_e2e(args.steps, stamps)
     ctx.mark(3)
     ms_e2e = max_over_ranks(ws, ctx.elapsed_ms(2, 3))
+    e2e_steps_ms = {name: 1e3 * statistics.mean(s[q] for s in stamps) if q < 5 else statistics.mean(s[q] for s in stamps)
+                    for q, name in enumerate(("input_copy", "build", "emit_queue", "wait_prev_copy", "close_prev",
+                                              "build_device"))}
     e2e_value = ws * args.steps * kmers / (ms_e2e / 1e3)
     link = host_link(local, len(w.text), out_bytes)
 
@@ -607,6 +622,7 @@ def run_gb300(args, ws, rank, local):
                 "pipelined": "job i's record copy to the host overlaps job i+1's input copy and build",
                 "host_link": link,
                 "link_bound_ms_per_step": (out_bytes / link["d2h_gbs"] + len(w.text) / link["h2d_gbs"]) / 1e6,
+                "host_ms_per_step": e2e_steps_ms,
                 "link_bound_note": "both copies through the host link one after the other: the bound if "
                                    "the link does not carry both directions at full rate at once"},
         "roofline": {"bound": "hbm", "kernel": "k_aggregate", "achieved": agg_achieved, "peak": peak,

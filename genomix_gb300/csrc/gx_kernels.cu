@@ -1980,7 +1980,7 @@ template <> struct AggTable<u128> {
 // cluster (a cluster that wraps past the last slot is numbered last).  Five phases with a
 // barrier between them:
 //   1. read heads (which claim or find their k-mer's slot and mark the set they belong to)
-//      and occurrences inserted: count += 1, edge bits OR-ed in only when new;
+//      and occurrences inserted: count += 1, edge bits OR-ed in;
 //   2. occupancy bitmap (warp ballots) and per-warp counts;
 //   3. every node's rank: its cluster's start, the occupied slots before it, its place by key
 //      in the cluster; key, count/meta word and base record size out;
@@ -1993,7 +1993,8 @@ template <> struct AggTable<u128> {
 template <class K>
 struct AggSmem {
     K key1[AGG_SLOTS];                 // key + 1; 0 = empty
-    unsigned long long cm[AGG_SLOTS];  // count | meta << 32 (edge bits, read-head set flags)
+    uint32_t cnt[AGG_SLOTS];           // occurrences
+    uint32_t meta[AGG_SLOTS];          // edge bits, read-head set flags
     uint32_t nbytes[AGG_SLOTS];        // record bytes per node in rank order, then offsets
     uint16_t ord[AGG_SLOTS];           // slot of the node of each rank
     uint16_t rank_of_slot[AGG_SLOTS];
@@ -2117,8 +2118,10 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         const uint4 z = make_uint4(0, 0, 0, 0);
         uint4 *k4 = reinterpret_cast<uint4 *>(sm.key1);
         for (uint32_t i = threadIdx.x; i < AGG_SLOTS * sizeof(K) / 16; i += blockDim.x) k4[i] = z;
-        uint4 *c4 = reinterpret_cast<uint4 *>(sm.cm);
-        for (uint32_t i = threadIdx.x; i < AGG_SLOTS / 2; i += blockDim.x) c4[i] = z;
+        for (uint32_t i = threadIdx.x; i < AGG_SLOTS / 4; i += blockDim.x) {
+            reinterpret_cast<uint4 *>(sm.cnt)[i] = z;
+            reinterpret_cast<uint4 *>(sm.meta)[i] = z;
+        }
     }
     if (threadIdx.x == 0) {
         sm.n = 0;
@@ -2138,8 +2141,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
                 p_h.slot = 0;
             } else {
                 if (claimed) atomicAdd(&sm.n, 1u);
-                atomicOr(&sm.cm[sl], (unsigned long long)((p_h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED)
-                                         << 32);
+                atomicOr(&sm.meta[sl], (p_h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
                 p_h.slot = (uint32_t)sl;
             }
         }
@@ -2155,7 +2157,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
                 continue;
             }
             if (claimed) atomicAdd(&sm.n, 1u);
-            atomicOr(&sm.cm[sl], (unsigned long long)((h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED) << 32);
+            atomicOr(&sm.meta[sl], (h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
             a.heads[r].slot = (uint32_t)sl;
         }
     }
@@ -2179,8 +2181,8 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
                 continue;
             }
             if (claimed) atomicAdd(&sm.n, 1u);
-            const unsigned long long old = atomicAdd(&sm.cm[sl], 1ULL);
-            if (bb[q] & ~(uint32_t)(old >> 32)) atomicOr(&sm.cm[sl], (unsigned long long)bb[q] << 32);
+            atomicAdd(&sm.cnt[sl], 1u);  // no result used: both are fire-and-forget reductions
+            if (bb[q]) atomicOr(&sm.meta[sl], bb[q]);
         }
     }
     __syncthreads();
@@ -2240,13 +2242,12 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         }
         sm.rank_of_slot[slot] = (uint16_t)rank;
         sm.ord[rank] = (uint16_t)slot;
-        const unsigned long long cmv = sm.cm[slot];
+        const uint32_t cnt = sm.cnt[slot], meta = sm.meta[slot];
         nkey[rank] = mine - 1;
-        ncm[rank] = cmv;
-        const uint32_t cnt = (uint32_t)cmv;
+        ncm[rank] = (unsigned long long)cnt | ((unsigned long long)meta << 32);
         if (cnt >= (1u << 24)) inexact++;
         if (cnt == 0) phantom++;  // a read head whose k-mer has no occurrence here
-        sm.nbytes[rank] = node_base_bytes((uint32_t)(cmv >> 32), nb);
+        sm.nbytes[rank] = node_base_bytes(meta, nb);
     }
     if (inexact) atomicAdd(&a.st->cov_inexact, inexact);
     if (phantom) atomicAdd(&a.st->internal_err, phantom);
@@ -2331,7 +2332,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             if (wkeep) {
                 const int first = __ffs(node_mask) - 1;
                 const uint32_t cu = __popc(node_mask & ~flip_mask), cf = __popc(node_mask & flip_mask);
-                const uint32_t meta = (uint32_t)(sm.cm[w_slot] >> 32);
+                const uint32_t meta = sm.meta[w_slot];
                 const uint32_t st = __popc(wkeep_mask & ((1u << first) - 1u));  // kept index of the node's first
                 HeadOut ho;
                 ho.uuid = w_uuid;
@@ -2470,7 +2471,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         const uint32_t cu = fl - st, cf = kept_lower_bound(hk, kept, rbase + (1ULL << 37)) - fl;
         const unsigned long long pre = key & ((1ULL << 36) - 1);
         const unsigned long long pre0 = hk[st] & ((1ULL << 36) - 1);
-        const uint32_t meta = (uint32_t)(sm.cm[sm.ord[rank]] >> 32);
+        const uint32_t meta = sm.meta[sm.ord[rank]];
         const uint32_t pos = sm.nbytes[rank] + 8 + keylen + 1 + edge_bytes(meta, nb) + 5 +
                              ((flipped && cu > 0) ? 5 : 0) + (uint32_t)(pre - pre0);
         const uint32_t r = hv[i];
