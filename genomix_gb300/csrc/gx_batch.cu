@@ -265,6 +265,8 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         if ((e = tar.alloc(head_off, P)) != GX_OK) return e;
         if ((e = tar.alloc(head_cur, P)) != GX_OK) return e;
         if ((e = tar.alloc(head_idx, n_reads)) != GX_OK) return e;
+        HeadIn *hsorted;
+        if ((e = tar.alloc(hsorted, n_reads)) != GX_OK) return e;
         if ((e = tar.alloc(head_cnt2, P)) != GX_OK) return e;
         if ((e = tar.alloc(head_sk, n_reads)) != GX_OK) return e;
         if ((e = tar.alloc(part_nodes, P)) != GX_OK) return e;
@@ -291,7 +293,7 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
                              0xffffffffu, nullptr, nullptr, s);
         launch_heads_part(wide, text, n_text, lines, reads, n_reads, k, smap, heads, head_cnt, s);
         exclusive_scan_u32(head_cnt, head_off, P, nullptr, pscratch, s);
-        launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, P, s);
+        launch_head_scatter_part(heads, reads, lines, n_reads, head_off, head_cur, head_idx, hsorted, s);
         launch_fine_count(wide, okey, d_chunks, n_chunks, d_sinfo, fine_cnt, s);
         exclusive_scan_u64(fine_cnt, fine_off, P, fine_off + P, pscratch, s);
         launch_scatter_fine(wide, okey, obits, d_chunks, n_chunks, d_sinfo, fine_off, fine_cur, okey2, obits2, s);
@@ -307,6 +309,7 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         g.reads = reads;
         g.heads = heads;
         g.head_idx = head_idx;
+        g.hsorted = hsorted;
         g.head_sk = head_sk;
         g.head_off = head_off;
         g.head_cnt = head_cnt;

@@ -254,6 +254,19 @@ struct Head {
     unsigned long long klo, khi;  // canonical first k-mer (the partitioned build looks it up)
 };
 
+// A read head gathered into its bucket's order for the partitioned build's aggregation: the
+// first k-mer, the uuid, and the read's text (offsets and lengths of the read and its mate),
+// so one load brings the aggregation everything it needs.
+struct __align__(16) HeadIn {
+    unsigned long long uuid;
+    unsigned long long klo, khi;      // canonical first k-mer
+    unsigned long long s_off, m_off;  // text offsets of the read and of its mate
+    uint32_t L, Lm;                   // read and mate lengths (Lm = 0: no mate sequence)
+    uint32_t r;                       // read ordinal (orders read heads with equal uuids)
+    uint32_t pad0;
+    unsigned long long pad1;
+};
+
 // A read head as the record writer needs it, in the partition's output order (partitioned
 // build): the head's byte position in its partition's records and, on the first head of a
 // set, the set's size.

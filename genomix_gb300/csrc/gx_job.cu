@@ -919,6 +919,8 @@ static gx_status build_partitioned(RunCtx &rc) {
         if ((e = tar.alloc(hout, n_reads)) != GX_OK) return e;
         if ((e = tar.alloc(noff, n_occ)) != GX_OK) return e;
         if ((e = tar.alloc(head_idx, n_reads)) != GX_OK) return e;
+        HeadIn *hsorted;
+        if ((e = tar.alloc(hsorted, n_reads)) != GX_OK) return e;
         if ((e = tar.alloc(head_sk, n_reads)) != GX_OK) return e;
         // the job is a batch of one sample
         SamplePlan *d_plan;
@@ -1035,7 +1037,7 @@ static gx_status build_partitioned(RunCtx &rc) {
         // read heads
         launch_heads_part(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, heads, head_cnt, s);
         exclusive_scan_u32(head_cnt, head_off, P, nullptr, pscratch, s);
-        launch_head_scatter(heads, n_reads, head_off, head_cur, head_idx, P, s);
+        launch_head_scatter_part(heads, rc.reads, rc.lines, n_reads, head_off, head_cur, head_idx, hsorted, s);
         // B1, B2
         launch_fine_count(wide, okey, d_chunks, n_chunks, d_sinfo, fine_cnt, s);
         exclusive_scan_u64(fine_cnt, fine_off, P, fine_off + P, pscratch, s);
@@ -1053,6 +1055,7 @@ static gx_status build_partitioned(RunCtx &rc) {
         g.reads = rc.reads;
         g.heads = heads;
         g.head_idx = head_idx;
+        g.hsorted = hsorted;
         g.head_sk = head_sk;
         g.head_off = head_off;
         g.head_cnt = head_cnt;

@@ -628,6 +628,40 @@ void launch_head_scatter(const Head *heads, uint32_t n_reads, const uint32_t *he
     k_head_scatter<<<(n_reads + 255) / 256, 256, 0, s>>>(heads, n_reads, head_off, head_cur, head_idx);
 }
 
+__global__ void k_head_scatter_part(const Head *heads, const uint32_t *reads, const LineRec *lines,
+                                    uint32_t n_reads, const uint32_t *head_off, uint32_t *head_cur,
+                                    uint32_t *head_idx, HeadIn *hsorted) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_reads) return;
+    const Head h = heads[r];
+    if (h.part == 0xffffffffu) return;
+    const uint32_t rl = reads[r], mate = rl & 1u;
+    const LineRec lr = lines[rl >> 1];
+    const uint32_t pos = head_off[h.part] + atomicAdd(&head_cur[h.part], 1u);
+    head_idx[pos] = r;
+    HeadIn hi;
+    hi.uuid = h.uuid;
+    hi.klo = h.klo;
+    hi.khi = h.khi;
+    hi.s_off = mate ? lr.s1 : lr.s0;
+    hi.m_off = mate ? lr.s0 : lr.s1;
+    hi.L = mate ? lr.l1 : lr.l0;
+    hi.Lm = mate ? lr.l0 : lr.l1;
+    hi.r = r;
+    hi.pad0 = 0;
+    hi.pad1 = 0;
+    hsorted[pos] = hi;
+}
+
+void launch_head_scatter_part(const Head *heads, const uint32_t *reads, const LineRec *lines, uint32_t n_reads,
+                              const uint32_t *head_off, uint32_t *head_cur, uint32_t *head_idx, HeadIn *hsorted,
+                              cudaStream_t s) {
+    if (!n_reads) return;
+    t_launches++;
+    k_head_scatter_part<<<(n_reads + 255) / 256, 256, 0, s>>>(heads, reads, lines, n_reads, head_off, head_cur,
+                                                              head_idx, hsorted);
+}
+
 // =========================================================================================
 // K4 + K5: emission, one CTA per table partition.
 //   prepare: compact occupied slots, sort them by canonical key, write them back to the
@@ -1972,6 +2006,17 @@ template <> struct AggTable<u128> {
     }
 };
 
+// Home slot of a key in a bucket's shared table: the top 11 bits of a multiplicative hash (the
+// bucket itself was picked by other bits of the MurmurHash3 finaliser).
+__device__ __forceinline__ uint32_t agg_home(uint64_t v) {
+    return (uint32_t)((v * 0x9E3779B97F4A7C15ULL) >> (64 - 11));
+}
+__device__ __forceinline__ uint32_t agg_home(u128 v) {
+    const uint64_t x = (uint64_t)v ^ ((uint64_t)(v >> 64) * 0xC2B2AE3D27D4EB4FULL);
+    return (uint32_t)((x * 0x9E3779B97F4A7C15ULL) >> (64 - 11));
+}
+static_assert(AGG_SLOTS == 1u << 11, "agg_home gives 11-bit slots");
+
 // One fine bucket per CTA.  The bucket's distinct k-mers are counted in a shared-memory
 // open-addressing table (linear probing), then put in a deterministic order without sorting:
 // with linear probing the set of occupied slots, and the set of keys in each cluster (maximal
@@ -2097,15 +2142,9 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
     // head i's entry, its read and the read's line now, so the loads land while the table clears.
     const uint32_t hb = a.head_off[f], hc = a.head_cnt[f];
     const bool warp_heads = hc <= 32;
-    uint32_t p_r = 0xffffffffu, p_rl = 0;
-    Head p_h{};
-    LineRec p_lr{};
-    if (warp_heads && threadIdx.x < hc) {
-        p_r = a.head_idx[hb + threadIdx.x];
-        p_h = a.heads[p_r];
-        p_rl = a.reads[p_r];
-        p_lr = a.lines[p_rl >> 1];
-    }
+    HeadIn p_h{};
+    uint32_t p_slot = 0;
+    if (warp_heads && threadIdx.x < hc) p_h = a.hsorted[hb + threadIdx.x];
     K kk[AGG_BATCH];
     uint32_t bb[AGG_BATCH];
 #pragma unroll
@@ -2135,14 +2174,13 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         if (threadIdx.x < hc) {
             const K key = (K)(((u128)p_h.khi << 64) | p_h.klo);
             uint32_t claimed = 0;
-            const int sl = AggTable<K>::insert(sm.key1, key, (uint32_t)KeyOps<K>::hash(key), claimed);
+            const int sl = AggTable<K>::insert(sm.key1, key, agg_home(key), claimed);
             if (sl < 0) {
                 sm.fail = 1;
-                p_h.slot = 0;
             } else {
                 if (claimed) atomicAdd(&sm.n, 1u);
                 atomicOr(&sm.meta[sl], (p_h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
-                p_h.slot = (uint32_t)sl;
+                p_slot = (uint32_t)sl;
             }
         }
     } else {
@@ -2151,7 +2189,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             const Head h = a.heads[r];
             const K key = (K)(((u128)h.khi << 64) | h.klo);
             uint32_t claimed = 0;
-            const int sl = AggTable<K>::insert(sm.key1, key, (uint32_t)KeyOps<K>::hash(key), claimed);
+            const int sl = AggTable<K>::insert(sm.key1, key, agg_home(key), claimed);
             if (sl < 0) {
                 sm.fail = 1;
                 continue;
@@ -2175,7 +2213,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
             if (i >= M) continue;
             uint32_t claimed = 0;
-            const int sl = AggTable<K>::insert(sm.key1, kk[q], (uint32_t)KeyOps<K>::hash(kk[q]), claimed);
+            const int sl = AggTable<K>::insert(sm.key1, kk[q], agg_home(kk[q]), claimed);
             if (sl < 0) {
                 sm.fail = 1;
                 continue;
@@ -2218,22 +2256,45 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
     K *nkey = (K *)a.nkey + o0;
     unsigned long long *ncm = a.ncm + o0;
     uint32_t inexact = 0, phantom = 0;
-#pragma unroll 2
-    for (int q = 0; q < 8; q++) {
-        const uint32_t word = __shfl_sync(full, myocc, q);
-        const uint32_t wpre = __shfl_sync(full, pc_incl - pc, q);
-        const uint32_t slot = warp * 256 + q * 32 + lane;
-        if (!((word >> lane) & 1u)) continue;
-        const uint32_t before = wbase + wpre + __popc(word & ((1u << lane) - 1u));  // occupied slots before
-        const uint32_t c0 = cluster_start(sm.occ, slot);
-        // occupied slots before the cluster: the run from c0 to this slot is all occupied; a
-        // cluster that wraps past the last slot occupies everything from c0 to the end
-        const uint32_t pre_c0 = c0 <= slot ? before - (slot - c0) : n - (AGG_SLOTS - c0);
+    // the warp's occupied slots, 32 at a time: lane i takes the i-th (its word by the words'
+    // running counts, its bit by a popcount search)
+    uint32_t winc[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) winc[q] = __shfl_sync(full, pc_incl, q);
+    const uint32_t wocc = winc[7];
+    for (uint32_t idx = lane; idx < wocc + ((32 - (wocc & 31)) & 31); idx += 32) {
+        uint32_t q = 0;
+#pragma unroll
+        for (int j = 0; j < 7; j++) q += winc[j] <= idx ? 1u : 0u;
+        const uint32_t word = __shfl_sync(full, myocc, (int)q);
+        const uint32_t wexcl = __shfl_sync(full, pc_incl - pc, (int)q);
+        if (idx >= wocc) continue;
+        uint32_t m = idx - wexcl, w = word, bit = 0;
+#pragma unroll
+        for (uint32_t sh = 16; sh; sh >>= 1) {
+            const uint32_t lo = __popc(w & ((1u << sh) - 1u));
+            if (m >= lo) {
+                m -= lo;
+                w >>= sh;
+                bit += sh;
+            }
+        }
+        const uint32_t slot = warp * 256 + q * 32 + bit;
+        const uint32_t before = wbase + idx;  // occupied slots before this one
         const K mine = sm.key1[slot];
-        uint32_t within = 0;
-        for (uint32_t j = c0;; j = (j + 1) & (AGG_SLOTS - 1)) {
-            if (!((sm.occ[j >> 5] >> (j & 31)) & 1u)) break;
-            within += sm.key1[j] < mine ? 1u : 0u;
+        const uint32_t sl_prev = (slot - 1) & (AGG_SLOTS - 1), sl_next = (slot + 1) & (AGG_SLOTS - 1);
+        uint32_t pre_c0, within = 0;
+        if (!((sm.occ[sl_prev >> 5] >> (sl_prev & 31)) & 1u) && !((sm.occ[sl_next >> 5] >> (sl_next & 31)) & 1u)) {
+            pre_c0 = before;  // a cluster of one
+        } else {
+            const uint32_t c0 = cluster_start(sm.occ, slot);
+            // occupied slots before the cluster: the run from c0 to this slot is all occupied; a
+            // cluster that wraps past the last slot occupies everything from c0 to the end
+            pre_c0 = c0 <= slot ? before - (slot - c0) : n - (AGG_SLOTS - c0);
+            for (uint32_t j = c0;; j = (j + 1) & (AGG_SLOTS - 1)) {
+                if (!((sm.occ[j >> 5] >> (j & 31)) & 1u)) break;
+                within += sm.key1[j] < mine ? 1u : 0u;
+            }
         }
         const uint32_t rank = pre_c0 - z + within;
         if (rank >= n) {  // never expected: the ranks are a permutation of [0, n)
@@ -2266,8 +2327,8 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             unsigned long long mk = ~0ULL;
             uint32_t mv = 0xffffffffu;
             if (lane < (int)hc) {
-                mv = p_r;
-                mk = head_sort_key(sm.rank_of_slot[p_h.slot], p_h.uuid);
+                mv = p_h.r;
+                mk = head_sort_key(sm.rank_of_slot[p_slot], p_h.uuid);
             }
             uint32_t rank = 0;
             for (int j = 0; j < (int)hc; j++) {
@@ -2285,13 +2346,12 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
                 wk = sm.wsk[lane];
                 src = sm.wsv[lane];
             }
-            const uint32_t mate = p_rl & 1u;
             w_uuid = shfl64(p_h.uuid, (int)src);
-            w_soff = shfl64(mate ? p_lr.s1 : p_lr.s0, (int)src);
-            w_moff = shfl64(mate ? p_lr.s0 : p_lr.s1, (int)src);
-            w_L = __shfl_sync(full, mate ? p_lr.l1 : p_lr.l0, (int)src);
-            w_Lm = __shfl_sync(full, mate ? p_lr.l0 : p_lr.l1, (int)src);
-            w_slot = __shfl_sync(full, p_h.slot, (int)src);
+            w_soff = shfl64(p_h.s_off, (int)src);
+            w_moff = shfl64(p_h.m_off, (int)src);
+            w_L = __shfl_sync(full, p_h.L, (int)src);
+            w_Lm = __shfl_sync(full, p_h.Lm, (int)src);
+            w_slot = __shfl_sync(full, p_slot, (int)src);
             const unsigned long long prev = shfl64(wk, lane > 0 ? lane - 1 : 0);
             wkeep = (lane < (int)hc && (lane == 0 || wk != prev)) ? 1u : 0u;
             wkeep_mask = __ballot_sync(full, wkeep);

@@ -61,6 +61,11 @@ void launch_insert(const TableGeom &g, const uint8_t *text, const LineRec *lines
                    uint32_t n_reads, int k, Head *heads, uint32_t *head_cnt, DevStatus *st, cudaStream_t s);
 void launch_head_scatter(const Head *heads, uint32_t n_reads, const uint32_t *head_off, uint32_t *head_cur,
                          uint32_t *head_idx, uint32_t nparts, cudaStream_t s);
+// The same scatter for the partitioned build, which also gathers each head's HeadIn record
+// into hsorted (same positions as head_idx).
+void launch_head_scatter_part(const Head *heads, const uint32_t *reads, const LineRec *lines, uint32_t n_reads,
+                              const uint32_t *head_off, uint32_t *head_cur, uint32_t *head_idx, HeadIn *hsorted,
+                              cudaStream_t s);
 
 // ---- emission ---------------------------------------------------------------------------
 struct EmitArgs {
@@ -177,6 +182,7 @@ struct AggArgs {
     const uint32_t *reads;
     Head *heads;
     uint32_t *head_idx;
+    const HeadIn *hsorted;      // the heads in bucket order (positions of head_idx)
     unsigned long long *head_sk;
     const uint32_t *head_off;
     const uint32_t *head_cnt;
