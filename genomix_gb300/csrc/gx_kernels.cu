@@ -1617,8 +1617,8 @@ struct SuperSmem {
     uint32_t ws[33];
     uint32_t rounds, total;
     uint32_t hll[SC_HLL_REGS];  // this block's HyperLogLog registers (when the build asks for them)
-    uint32_t arrays[1];  // loff[S], gbase[S], cur[S]
-    static size_t bytes(uint32_t S) { return sizeof(SuperSmem) + 3ull * S * sizeof(uint32_t); }
+    uint32_t arrays[1];  // loff[S], gbase[S], cur[S], glo[S]
+    static size_t bytes(uint32_t S) { return sizeof(SuperSmem) + 4ull * S * sizeof(uint32_t); }
 };
 
 // 64-bit keys keep a round's k-mers in registers between counting and placing them; 128-bit
@@ -1641,6 +1641,7 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
     extern __shared__ __align__(16) uint8_t smem_raw[];
     SuperSmem<K> &sm = *reinterpret_cast<SuperSmem<K> *>(smem_raw);
     uint32_t *const sm_loff = sm.arrays, *const sm_gbase = sm.arrays + S, *const sm_cur = sm.arrays + 2 * S;
+    uint32_t *const sm_glo = sm.arrays + 3 * S;
     const uint32_t r = blockIdx.x * SC_THREADS + threadIdx.x;
     Walker<K> w;
     uint32_t sbase = 0, log_s = 0;
@@ -1699,7 +1700,17 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
         }
         __syncthreads();
         const uint32_t tot = block_scan_array(sm_loff, S, sm.ws);
-        for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) sm_cur[i] = 0;
+        // element i of bucket sp goes to s_off[sp] + gbase[sp] + (i - loff[sp]): the base, as
+        // gbase (high word, ~0 for a bucket out of room) and glo (low word)
+        for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) {
+            sm_cur[i] = 0;
+            const uint32_t g = sm_gbase[i];
+            if (g != 0xffffffffu) {
+                const unsigned long long b = s_off[i] + g - sm_loff[i];
+                sm_glo[i] = (uint32_t)b;
+                sm_gbase[i] = (uint32_t)(b >> 32);
+            }
+        }
         __syncthreads();
         // place them in shared memory grouped by super bucket
         if (!CACHE) w = w0;
@@ -1725,9 +1736,9 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
         __syncthreads();
         // write the runs out
         for (uint32_t i = threadIdx.x; i < tot; i += blockDim.x) {
-            const uint32_t sp = sm.sup[i];
-            if (sm_gbase[sp] == 0xffffffffu) continue;
-            const unsigned long long g = s_off[sp] + sm_gbase[sp] + (i - sm_loff[sp]);
+            const uint32_t sp = sm.sup[i], hi = sm_gbase[sp];
+            if (hi == 0xffffffffu) continue;
+            const unsigned long long g = (((unsigned long long)hi << 32) | sm_glo[sp]) + i;
             okey[g] = sm.key[i];
             obits[g] = sm.bits[i];
         }
@@ -1873,7 +1884,15 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 3 : 2) k_scatter_fine(co
     }
     __syncthreads();
     block_scan_array(sm.loff, F, sm.ws);
-    for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) sm.cur[i] = 0;
+    // Element i of bucket b (staged at loff[b] + its rank) goes to fine_off[f0 + b] + gbase[b] +
+    // rank = base0 + gbase'[b] + i, with gbase'[b] = fine_off[f0 + b] - base0 + gbase[b] - loff[b]:
+    // never negative (loff[b] counts this chunk's part of the buckets before b) and below the
+    // super bucket's 32-bit size, so the write-out needs no global load per element.
+    const unsigned long long base0 = fine_off[f0];
+    for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) {
+        sm.cur[i] = 0;
+        sm.gbase[i] = (uint32_t)(fine_off[f0 + i] - base0) + sm.gbase[i] - sm.loff[i];
+    }
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < FINE_PER_THREAD; q++) {
@@ -1886,8 +1905,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 3 : 2) k_scatter_fine(co
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
-        const uint32_t b = sm.bkt[i];
-        const unsigned long long g = fine_off[f0 + b] + sm.gbase[b] + (i - sm.loff[b]);
+        const unsigned long long g = base0 + sm.gbase[sm.bkt[i]] + i;
         okey2[g] = sm.key[i];
         obits2[g] = sm.bits[i];
     }
