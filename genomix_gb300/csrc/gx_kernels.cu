@@ -2149,6 +2149,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
     extern __shared__ __align__(16) uint8_t smem_raw[];
     AggSmem<K> &sm = *reinterpret_cast<AggSmem<K> *>(smem_raw);
     const unsigned full = 0xffffffffu;
+    constexpr int BATCH = sizeof(K) == 8 ? AGG_BATCH : AGG_BATCH / 2;  // occurrence loads in flight per thread
     const uint32_t f = blockIdx.x;
     const int nb = (a.k + 3) / 4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -2163,10 +2164,10 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
     HeadIn p_h{};
     uint32_t p_slot = 0;
     if (warp_heads && threadIdx.x < hc) p_h = a.hsorted[hb + threadIdx.x];
-    K kk[AGG_BATCH];
-    uint32_t bb[AGG_BATCH];
+    K kk[BATCH];
+    uint32_t bb[BATCH];
 #pragma unroll
-    for (int q = 0; q < AGG_BATCH; q++) {
+    for (int q = 0; q < BATCH; q++) {
         const uint32_t i = q * blockDim.x + threadIdx.x;
         kk[q] = i < M ? okey[i] : (K)0;
         bb[q] = i < M ? (uint32_t)obits[i] : 0u;
@@ -2217,28 +2218,45 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             a.heads[r].slot = (uint32_t)sl;
         }
     }
-    for (uint32_t c0 = 0; c0 < M; c0 += AGG_BATCH * blockDim.x) {
+    for (uint32_t c0 = 0; c0 < M; c0 += BATCH * blockDim.x) {
         if (c0) {
 #pragma unroll
-            for (int q = 0; q < AGG_BATCH; q++) {
+            for (int q = 0; q < BATCH; q++) {
                 const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
                 kk[q] = i < M ? okey[i] : (K)0;
                 bb[q] = i < M ? (uint32_t)obits[i] : 0u;
             }
         }
+        // In groups of four: the home slots are read first, all four loads in flight (a key
+        // never leaves the slot it was put in, so a plain read that shows it is final); an
+        // occurrence whose key is not in its home slot takes the probe with compare-and-swap.
 #pragma unroll
-        for (int q = 0; q < AGG_BATCH; q++) {
-            const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
-            if (i >= M) continue;
-            uint32_t claimed = 0;
-            const int sl = AggTable<K>::insert(sm.key1, kk[q], agg_home(kk[q]), claimed);
-            if (sl < 0) {
-                sm.fail = 1;
-                continue;
+        for (int g = 0; g < BATCH; g += 4) {
+            uint32_t hm[4];
+            K cur[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                hm[u] = agg_home(kk[g + u]);
+                cur[u] = sm.key1[hm[u]];
             }
-            if (claimed) atomicAdd(&sm.n, 1u);
-            atomicAdd(&sm.cnt[sl], 1u);  // no result used: both are fire-and-forget reductions
-            if (bb[q]) atomicOr(&sm.meta[sl], bb[q]);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int q = g + u;
+                const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
+                if (i >= M) continue;
+                int sl = (int)hm[u];
+                if (cur[u] != kk[q] + 1) {
+                    uint32_t claimed = 0;
+                    sl = AggTable<K>::insert(sm.key1, kk[q], hm[u], claimed);
+                    if (sl < 0) {
+                        sm.fail = 1;
+                        continue;
+                    }
+                    if (claimed) atomicAdd(&sm.n, 1u);
+                }
+                atomicAdd(&sm.cnt[sl], 1u);  // no result used: both are fire-and-forget reductions
+                if (bb[q]) atomicOr(&sm.meta[sl], bb[q]);
+            }
         }
     }
     __syncthreads();
