@@ -14,11 +14,12 @@ reads, see genomix_gb300/synth.py).
   e2e        the same metric through the C ABI with host buffers: pinned readid text in,
              H2D copy, build, D2H copy of every record into pinned memory, per step; steps
              are pipelined (gx_job_emit_async): step i's copy out overlaps step i+1's build
-  roofline   the dominant kernel of the build, the record writer (k_emit_write_part, about
-             40% of the device time): its algorithmic bytes per launch (the record stream
-             written, plus the compacted nodes and read heads it reads) over its CUDA-event
-             duration, against the measured HBM copy bandwidth; `random_access` gives
-             k-mers/s against the hash-table random-access bound (64 B per occurrence)
+  roofline   the largest kernel of the build, the per-bucket aggregation (k_aggregate): its
+             algorithmic bytes per launch (every occurrence's key and edge bits read, each
+             node's key, count/meta word and record offset written, each read head's entries)
+             over its CUDA-event duration, against the measured HBM copy bandwidth;
+             `roofline_writer` does the same for the record writer pair, and `random_access`
+             gives k-mers/s against the hash-table random-access bound (64 B per occurrence)
   cpu_baseline  the oracle (C++ restatement of the reference's sort + group graph build) on
              the first pairs of the same workload, all host threads
   batched    the 64-sample workload (genomes log-uniform 20 kbp - 2 Mbp, 10-60x single-end
@@ -52,8 +53,8 @@ CPU_SAMPLE_PAIRS = 120_000   # cpu_baseline sample (one run)
 REF_STEP_PAIRS = 60_000      # --impl reference: sample per step
 TUNE_PAIRS = 200_000         # autotuner sample: the first pairs of the workload
 LAYOUT_PARTS = 16            # parts of the reference part layout measurement
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_emit_write_part_pe5mbp_k31.md")
-PROFILE_TRAFFIC_AGG = os.path.join(ROOT, "profiles", "k_aggregate_pe5mbp_k31.md")
+# DRAM bytes per algorithmic byte of each roofline kernel, from its committed ncu capture
+TRAFFIC_RATIOS = os.path.join(ROOT, "profiles", "traffic_ratios.json")
 AGG_HEAD_BYTES = 112         # per read head in k_aggregate: Head read and written, HeadOut, its read's line
 HEADOUT_BYTES = 48           # one HeadOut entry (uuid, two text offsets, position, counts)
 
@@ -67,17 +68,14 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(alg_bytes, path=PROFILE_TRAFFIC):
-    """DRAM bytes of one record-writer pass (the record writer and the read-head writer) from the
-    committed ncu summary: the capture runs a smaller case of the same workload, whose DRAM bytes
-    per algorithmic byte scale to this pass (the traffic grows in proportion to the records)."""
-    if not os.path.exists(path):
+def profiled_traffic(alg_bytes, kernel):
+    """DRAM bytes of one launch of `kernel` (a key of profiles/traffic_ratios.json): its ncu
+    capture ran a smaller case of the same workload, whose DRAM bytes per algorithmic byte scale
+    to the full launch (the traffic grows in proportion to the occurrences and records)."""
+    if not os.path.exists(TRAFFIC_RATIOS):
         return None
-    ratio = None
-    with open(path) as f:
-        for line in f:
-            if line.startswith("dram_bytes_per_algorithmic_byte:"):
-                ratio = float(line.split(":")[1])
+    with open(TRAFFIC_RATIOS) as f:
+        ratio = json.load(f).get(kernel, {}).get("dram_bytes_per_algorithmic_byte")
     return None if ratio is None else ratio * alg_bytes
 
 
@@ -232,6 +230,14 @@ SERVE_REQUESTS = 96                         # requests per rate, cycling through
 SERVE_CLIENTS = 4                           # client threads submitting the arrivals
 
 
+def pct(v, q):
+    """The q-quantile of the values (nearest rank); None for none."""
+    if not v:
+        return None
+    v = sorted(v)
+    return v[min(len(v) - 1, int(q * len(v)))]
+
+
 def bench_serving(ctx, works, rates=SERVE_RATES, n_req=SERVE_REQUESTS):
     """Poisson arrivals of graph-build jobs at each offered rate: client threads create each
     job at its arrival time (input copied from pinned host memory) and hand it to the server;
@@ -244,6 +250,8 @@ def bench_serving(ctx, works, rates=SERVE_RATES, n_req=SERVE_REQUESTS):
         p = gx.PinnedBuffer(len(w.text))
         p.array()[:] = memoryview(w.text)
         pins.append(p)
+    # jobs at or below the pool's median input size are "small", the rest "large"
+    median_bytes = sorted(len(w.text) for w in works)[len(works) // 2]
     out = []
     with gx.Server(ctx) as srv:
         # warm the lanes (first passes grow the memory pool), untimed
@@ -278,28 +286,30 @@ def bench_serving(ctx, works, rates=SERVE_RATES, n_req=SERVE_REQUESTS):
             for th in ths:
                 th.start()
             lat, kmers, t_end = [], 0, t0
+            lat_small, lat_large = [], []
             for i in range(n_req):
                 ready[i].wait()
                 st, srv_ms = srv.poll(tickets[i])
                 assert st == 0, st
                 lt = (t_sub[i] - (t0 + arr[i])) * 1e3 + srv_ms  # arrival -> done
                 lat.append(lt)
+                (lat_small if len(works[i % len(works)].text) <= median_bytes else lat_large).append(lt)
                 t_end = max(t_end, t0 + arr[i] + lt / 1e3)
                 kmers += jobs[i].stats()["kmers"]
                 jobs[i].close()
             for th in ths:
                 th.join()
             span = t_end - t0
-            lat.sort()
             out.append({"offered_jobs_per_s": rate, "jobs": n_req, "achieved_jobs_per_s": n_req / span,
-                        "kmers_per_s": kmers / span, "p50_ms": lat[len(lat) // 2],
-                        "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))]})
+                        "kmers_per_s": kmers / span, "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99),
+                        "p50_small_ms": pct(lat_small, 0.5), "p99_small_ms": pct(lat_small, 0.99),
+                        "p50_large_ms": pct(lat_large, 0.5), "p99_large_ms": pct(lat_large, 0.99)})
         st = srv.stats()
     for p in pins:
         p.close()
     sustained = [r for r in out if r["achieved_jobs_per_s"] >= 0.9 * r["offered_jobs_per_s"]]
     top = max(sustained, key=lambda r: r["offered_jobs_per_s"]) if sustained else None
-    return {"workload": "serving_pe150_30x_k21_31_55", "job_pool": len(works),
+    return {"workload": "serving_pe150_30x_k21_31_55", "job_pool": len(works), "median_job_bytes": median_bytes,
             "mean_job_bytes": sum(len(w.text) for w in works) / len(works), "rates": out,
             "highest_sustained": top, "passes": st["batches"], "max_jobs_per_pass": st["max_batch_jobs"]}
 
@@ -456,6 +466,25 @@ def bench_layout(ctx, w, d_text, warmup, pin, parts=LAYOUT_PARTS, reps=3):
             "record_bytes": rb, "alg_gbs": alg / (ms / 1e3) / 1e9}
 
 
+def compact_tune(t):
+    """The autotuner's choice without its per-candidate list (that goes to --details)."""
+    if not t:
+        return t
+    return {k: t[k] for k in ("algorithm", "load_factor", "ms") if k in t} | {"tried": len(t.get("candidates", []))}
+
+
+def compact_serving(srv):
+    """Serving summary for the bench line: per offered rate [offered, achieved jobs/s, p50 ms,
+    p99 ms], the highest sustained rate in full; the full per-rate records go to --details."""
+    if not srv:
+        return srv
+    out = {k: v for k, v in srv.items() if k != "rates"}
+    cols = ["offered_jobs_per_s", "achieved_jobs_per_s", "p50_ms", "p99_ms", "p99_small_ms", "p99_large_ms"]
+    out["rates"] = [[None if r[c] is None else round(r[c], 2) for c in cols] for r in srv["rates"]]
+    out["rates_columns"] = cols
+    return out
+
+
 def config_of(w, n):
     return {"workload": w.name, "genome_bp": w.genome_len, "pairs": w.reads, "read_len": 150, "k": w.k,
             "input_bytes": len(w.text), "parallelism": f"replicas{n}" if n > 1 else "single",
@@ -601,7 +630,7 @@ def run_gb300(args, ws, rank, local):
     wr_ms = statistics.mean(s["ms_write"] for s in stats)
     wr_bytes = writer_alg_bytes(stats[0], w.k, 150, True)
     achieved = wr_bytes / (wr_ms / 1e3) / 1e9
-    traffic = profiled_traffic(wr_bytes)
+    traffic = profiled_traffic(wr_bytes, "k_emit_write_part+k_write_heads_part")
     agg_ms = statistics.mean(s["ms_aggregate"] for s in stats)
     agg_bytes = aggregate_alg_bytes(stats[0], w.k)
     agg_achieved = agg_bytes / (agg_ms / 1e3) / 1e9
@@ -627,7 +656,7 @@ def run_gb300(args, ws, rank, local):
                                    "the link does not carry both directions at full rate at once"},
         "roofline": {"bound": "hbm", "kernel": "k_aggregate", "achieved": agg_achieved, "peak": peak,
                      "unit": "GB/s", "frac": agg_achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth",
-                     "traffic": profiled_traffic(agg_bytes, PROFILE_TRAFFIC_AGG), "alg_bytes_per_launch": agg_bytes,
+                     "traffic": profiled_traffic(agg_bytes, "k_aggregate"), "alg_bytes_per_launch": agg_bytes,
                      "ms_per_launch": agg_ms,
                      "unit_of_work": "k-mer occurrence aggregated (10 B read; 20 B per node and 112 B per read "
                                      "head written)"},
@@ -647,13 +676,16 @@ def run_gb300(args, ws, rank, local):
                   "read_heads": stats[0]["read_heads"], "record_bytes": out_bytes,
                   "table_slots": stats[0]["table_slots"], "max_probe": stats[0]["max_probe"]},
         "clocks": clk.summary(),
-        "autotune": tune,
+        "autotune": compact_tune(tune),
         "batched": bat,
-        "serving": srv,
-        "long_k": lk,
+        "serving": compact_serving(srv),
+        "long_k": dict(lk, autotune=compact_tune(lk["autotune"])) if lk else None,
         "reference_layout": lay,
         "cpu_baseline": cb,
     }
+    if args.details:
+        with open(args.details, "w") as f:
+            json.dump({"autotune": tune, "serving": srv, "long_k_autotune": lk["autotune"] if lk else None}, f)
     print(json.dumps(line), flush=True)
     pin_in.close()
     for b in outs:
@@ -675,6 +707,8 @@ def main():
     ap.add_argument("--no-layout", action="store_true", help="skip the reference part layout measurement")
     ap.add_argument("--fill", type=float, default=0.0,
                     help="partitioned build at this bucket fill instead of the autotuner's choice (profiling runs)")
+    ap.add_argument("--details", default=None,
+                    help="write the per-candidate and per-rate records to this JSON file")
     ap.add_argument("--max-pairs", type=int, default=None,
                     help="use only the first pairs of the workload (profiling captures)")
     args = ap.parse_args()

@@ -11,6 +11,9 @@ LIB_PATH = os.path.join(PKG, "libgxgpu.so")
 
 GX_OK = 0
 GX_EAGAIN = 14
+GX_ESTATE = 10
+GX_ECANCELLED = 11
+GX_EBUSY = 13
 STATUS_NAMES = {
     0: "GX_OK", 1: "GX_EINVAL", 2: "GX_EINVAL_LINE", 3: "GX_EINVAL_NUMBER", 4: "GX_EREADID_RANGE",
     5: "GX_EREAD_TOO_SHORT", 6: "GX_ENOMEM", 7: "GX_ETABLE_FULL", 8: "GX_ETIMEOUT", 9: "GX_ECUDA",
@@ -29,13 +32,15 @@ EXPORTS = [
     "gx_pinned_free", "gx_fastq_to_readid", "gx_host_free", "gx_seqfile_write", "gx_seqfile_read",
     "gx_records_to_text", "gx_build_noalloc",
     "gx_serve_create", "gx_serve_submit", "gx_serve_poll", "gx_serve_stats_get", "gx_serve_destroy",
+    "gx_serve_cancel",
     "gx_records_digest", "gx_autotune", "gx_autotune_clear", "gx_job_graph_stats", "gx_seqfile_write_kmer_keys",
     "gx_fastq_to_readid_gpu", "gx_job_emit_async", "gx_job_emit_wait",
 ]
 
 
 class CtxOpts(ctypes.Structure):
-    _fields_ = [("struct_size", ctypes.c_size_t), ("device_mem_limit", ctypes.c_size_t), ("flags", ctypes.c_int)]
+    _fields_ = [("struct_size", ctypes.c_size_t), ("device_mem_limit", ctypes.c_size_t), ("flags", ctypes.c_int),
+                ("test_alloc_fail_above", ctypes.c_size_t)]
 
 
 class JobOpts(ctypes.Structure):
@@ -57,12 +62,12 @@ class JobOpts(ctypes.Structure):
 
 class ServeOpts(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_size_t), ("mem_budget", ctypes.c_size_t), ("lanes", ctypes.c_int),
-                ("max_batch", ctypes.c_int)]
+                ("max_batch", ctypes.c_int), ("pass_bytes", ctypes.c_size_t)]
 
 
 class ServeStats(ctypes.Structure):
     _fields_ = [(f, ctypes.c_uint64) for f in ("jobs_submitted", "jobs_done", "batches", "max_batch_jobs",
-                                                "jobs_waiting", "jobs_running", "bytes_in_use")]
+                                                "jobs_waiting", "jobs_running", "bytes_in_use", "jobs_cancelled")]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -176,6 +181,7 @@ def load():
         "gx_serve_submit": ([vp, vp, P(ctypes.c_uint64)], i),
         "gx_serve_poll": ([vp, ctypes.c_uint64, i, P(i), P(ctypes.c_double)], i),
         "gx_serve_stats_get": ([vp, P(ServeStats)], i),
+        "gx_serve_cancel": ([vp, ctypes.c_uint64], i),
         "gx_serve_destroy": ([vp], None),
         "gx_records_digest": ([vp, sz, P(Digest)], i),
         "gx_autotune": ([vp, vp, sz, i, i, P(TuneResult)], i),

@@ -462,6 +462,7 @@ static gx_status batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses)
     if (!c || (!jobs && n) || n < 0) return GX_EINVAL;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaSetDevice(c->device);
+    const AllocLimitScope als(c->test_alloc_fail_above);
     std::map<gx_job *, gx_status> result;
     std::map<int, std::vector<gx_job *>> by_k;
     for (int i = 0; i < n; i++) {

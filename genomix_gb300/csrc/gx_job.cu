@@ -145,6 +145,8 @@ gx_status gx_ctx_create(int device, const gx_ctx_opts *opts, gx_ctx **out) {
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     c->mem_limit = (opts && opts->device_mem_limit) ? opts->device_mem_limit : (size_t)(0.9 * (double)fr);
+    if (opts && opts->struct_size >= offsetof(gx_ctx_opts, test_alloc_fail_above) + sizeof(size_t))
+        c->test_alloc_fail_above = opts->test_alloc_fail_above;
     for (auto &e : c->marks) cudaEventCreate(&e);
     if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaStreamDestroy(c->stream);
@@ -1345,7 +1347,10 @@ void gxi::ctx_release(gx_ctx *c) {
     delete c;
 }
 
+thread_local size_t gxi::t_alloc_fail_above = 0;
+
 gx_status gxi::run_job_locked(gx_job *j) {
+    const AllocLimitScope als(j->ctx->test_alloc_fail_above);
     const uint64_t l0 = launches_this_thread();
     gx_status st = guarded("gx_job_run", [&] { return run_job(j); });
     j->st.kernel_launches = launches_this_thread() - l0;

@@ -46,6 +46,7 @@ struct gx_ctx {
     cudaStream_t copy_stream = nullptr;  // gx_job_emit_async copies: they overlap the next build
     std::mutex mu;
     size_t mem_limit = 0;
+    size_t test_alloc_fail_above = 0;  // testing: run allocations above this fail as out of memory
     cudaEvent_t marks[16] = {};
     // the handle holds one reference and every job one more: a context destroyed while jobs
     // still live is freed with the last of them
@@ -102,6 +103,15 @@ struct gx_job {
 
 namespace gxi {
 
+// Set while a run executes on a context with gx_ctx_opts.test_alloc_fail_above (testing): run
+// allocations above it fail as if the device were out of memory.
+extern thread_local size_t t_alloc_fail_above;
+struct AllocLimitScope {
+    size_t saved;
+    explicit AllocLimitScope(size_t v) : saved(t_alloc_fail_above) { t_alloc_fail_above = v; }
+    ~AllocLimitScope() { t_alloc_fail_above = saved; }
+};
+
 // Allocations of one run, released together (stream ordered).
 struct RunArena {
     cudaStream_t s;
@@ -111,6 +121,7 @@ struct RunArena {
     gx_status alloc(T *&p, size_t count) {
         void *q = nullptr;
         const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+        if (t_alloc_fail_above && bytes > t_alloc_fail_above) return GX_ENOMEM;
         cudaError_t e = cudaMallocAsync(&q, bytes, s);
         if (e != cudaSuccess) {
             cudaGetLastError();

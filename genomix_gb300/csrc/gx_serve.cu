@@ -3,14 +3,18 @@
 // A server owns `lanes` contexts on one device, each with its own stream and one worker
 // thread.  Submitted jobs wait in one FIFO queue.  Whenever a lane is idle it admits, in
 // arrival order, every waiting job whose estimated device memory still fits the server's
-// budget (the oldest job is always admitted when nothing else is in flight, so a job larger
-// than the budget still runs, alone), up to `max_batch` jobs, and runs them as one
-// gx_batch_run pass.  Jobs that arrive while lanes are busy are picked up by the next lane
-// to free up: batches form continuously, and the passes of different lanes overlap on the
-// device.  Results stay device-resident in their jobs until the caller emits and destroys
+// budget and the pass's own cap (`pass_bytes`; the oldest job is always admitted when nothing
+// else is in flight, so a job larger than the budget still runs, alone), up to `max_batch`
+// jobs, and runs them as one gx_batch_run pass.  Every job of a pass finishes when the pass
+// does, so the cap keeps small jobs out of a large job's pass: the large one runs on a lane of
+// its own while the other lanes keep serving the small ones.  Jobs that arrive while lanes
+// are busy are picked up by the next lane to free up: batches form continuously, and the
+// passes of different lanes overlap on the device.  Results stay device-resident in their jobs until the caller emits and destroys
 // them.  While the server runs a job, the job belongs to it: call nothing on that job until
 // gx_serve_poll reports it done.
+#include <algorithm>
 #include <chrono>
+#include <cstddef>
 #include <condition_variable>
 #include <cstdio>
 #include <deque>
@@ -62,7 +66,7 @@ struct gx_server {
     std::deque<uint64_t> pending;
     std::unordered_map<uint64_t, Ticket> tickets;
     uint64_t next_id = 1;
-    size_t budget = 0, in_use = 0;
+    size_t budget = 0, in_use = 0, pass_bytes = 0;
     int max_batch = 64;
     int running = 0;
     bool stop = false;
@@ -96,6 +100,7 @@ static void lane_loop_impl(gx_server *sv, gx_ctx *lane) {
                 const size_t e = sv->tickets[id].est;
                 const bool alone = take.empty() && sv->in_use == 0;
                 if (!alone && sv->in_use + est + e > sv->budget) break;  // keep arrival order
+                if (!take.empty() && est + e > sv->pass_bytes) break;   // the pass is full
                 take.push_back(id);
                 est += e;
             }
@@ -146,16 +151,19 @@ gx_status gx_serve_create(gx_ctx *ctx, const gx_serve_opts *opts, gx_server **ou
 
 static gx_status serve_create_impl(gx_ctx *ctx, const gx_serve_opts *opts, gx_server **out) {
     if (!ctx || !out) return GX_EINVAL;
-    if (opts && opts->struct_size < sizeof(gx_serve_opts)) return GX_EINVAL;
+    // callers built against the struct before pass_bytes existed pass the shorter size
+    if (opts && opts->struct_size < offsetof(gx_serve_opts, pass_bytes)) return GX_EINVAL;
+    const bool has_pass = opts && opts->struct_size >= offsetof(gx_serve_opts, pass_bytes) + sizeof(size_t);
     *out = nullptr;
     gx_server *sv = new (std::nothrow) gx_server();
     if (!sv) return GX_ENOMEM;
     sv->device = ctx->device;
-    const int lanes = opts && opts->lanes > 0 ? opts->lanes : 2;
+    const int lanes = opts && opts->lanes > 0 ? opts->lanes : 4;
     sv->max_batch = opts && opts->max_batch > 0 ? opts->max_batch : 64;
     sv->budget = opts && opts->mem_budget ? opts->mem_budget : ctx->mem_limit;
+    sv->pass_bytes = has_pass && opts->pass_bytes ? opts->pass_bytes : (2ull << 30);
     for (int i = 0; i < lanes; i++) {
-        gx_ctx_opts co{sizeof(gx_ctx_opts), ctx->mem_limit, 0};
+        gx_ctx_opts co{sizeof(gx_ctx_opts), ctx->mem_limit, 0, ctx->test_alloc_fail_above};
         gx_ctx *c = nullptr;
         const gx_status st = gx_ctx_create(ctx->device, &co, &c);
         if (st != GX_OK) {
@@ -228,6 +236,24 @@ static gx_status serve_poll_impl(gx_server *sv, uint64_t ticket, int timeout_ms,
     sv->tickets.erase(ticket);
     if (job_status) *job_status = t.st;
     if (latency_ms) *latency_ms = t.t_done - t.t_submit;
+    return GX_OK;
+}
+
+gx_status gx_serve_cancel(gx_server *sv, uint64_t ticket) {
+    if (!sv) return GX_EINVAL;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->tickets.find(ticket);
+    if (it == sv->tickets.end()) return GX_EINVAL;
+    Ticket &t = it->second;
+    if (t.done) return GX_ESTATE;
+    auto q = std::find(sv->pending.begin(), sv->pending.end(), ticket);
+    if (q == sv->pending.end()) return GX_EBUSY;  // admitted: it runs to the end
+    sv->pending.erase(q);
+    t.st = GX_ECANCELLED;
+    t.t_done = now_ms();
+    t.done = true;
+    sv->stats.jobs_cancelled++;
+    sv->cv_done.notify_all();
     return GX_OK;
 }
 

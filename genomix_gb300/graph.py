@@ -89,10 +89,10 @@ class PinnedBuffer:
 class Context:
     """A device and its stream (replaces the Hyracks cluster-controller connection)."""
 
-    def __init__(self, device=0, mem_limit=0):
+    def __init__(self, device=0, mem_limit=0, test_alloc_fail_above=0):
         L = _lib.load()
         self._L = L
-        opts = _lib.CtxOpts(ctypes.sizeof(_lib.CtxOpts), mem_limit, 0)
+        opts = _lib.CtxOpts(ctypes.sizeof(_lib.CtxOpts), mem_limit, 0, int(test_alloc_fail_above))
         h = ctypes.c_void_p()
         _check(L.gx_ctx_create(device, ctypes.byref(opts), ctypes.byref(h)), "gx_ctx_create")
         self.h = h.value
@@ -291,10 +291,11 @@ class Server:
     memory over `lanes` concurrent passes.  submit() hands a job over; poll() returns
     (status, latency_ms) once it is done, or None while it is not."""
 
-    def __init__(self, ctx, mem_budget=0, lanes=0, max_batch=0):
+    def __init__(self, ctx, mem_budget=0, lanes=0, max_batch=0, pass_bytes=0):
         self.ctx = ctx
         self._L = ctx._L
-        o = _lib.ServeOpts(ctypes.sizeof(_lib.ServeOpts), int(mem_budget), int(lanes), int(max_batch))
+        o = _lib.ServeOpts(ctypes.sizeof(_lib.ServeOpts), int(mem_budget), int(lanes), int(max_batch),
+                           int(pass_bytes))
         h = ctypes.c_void_p()
         _check(self._L.gx_serve_create(ctx.h, ctypes.byref(o), ctypes.byref(h)), "gx_serve_create")
         self.h = h.value
@@ -316,6 +317,15 @@ class Server:
         if job is not None:
             job._keep.clear()
         return st.value, lat.value
+
+    def cancel(self, ticket):
+        """Withdraws a job that has not started (gx_serve_cancel): True when cancelled (its
+        poll() then reports GX_ECANCELLED), False when it is already running or done."""
+        r = self._L.gx_serve_cancel(self.h, ticket)
+        if r in (_lib.GX_EBUSY, _lib.GX_ESTATE):
+            return False
+        _check(r, "gx_serve_cancel")
+        return True
 
     def stats(self):
         s = _lib.ServeStats()

@@ -77,6 +77,10 @@ typedef struct gx_ctx_opts {
     size_t struct_size;       /* sizeof(gx_ctx_opts) */
     size_t device_mem_limit;  /* bytes the context may hold on the device; 0 = 90% of free */
     int flags;                /* reserved, 0 */
+    size_t test_alloc_fail_above; /* testing only: any working-buffer allocation of a run on this
+                                     context larger than this many bytes fails as if the device
+                                     were out of memory (0 = off); lets tests reach the
+                                     out-of-memory paths without exhausting the GPU */
 } gx_ctx_opts;
 
 typedef struct gx_job_opts {
@@ -297,8 +301,11 @@ typedef struct gx_server gx_server;
 typedef struct gx_serve_opts {
     size_t struct_size;  /* sizeof(gx_serve_opts) */
     size_t mem_budget;   /* device bytes the admitted jobs may use together; 0 = the context's limit */
-    int lanes;           /* passes in flight at once, each on its own stream; 0 = 2 */
+    int lanes;           /* passes in flight at once, each on its own stream; 0 = 4 */
     int max_batch;       /* jobs admitted into one pass; 0 = 64 */
+    size_t pass_bytes;   /* estimated device bytes one pass admits; its first job always goes in, so a
+                            job above this runs in a pass of its own and small jobs never wait for a
+                            large one's pass; 0 = 2 GiB */
 } gx_serve_opts;
 
 typedef struct gx_serve_stats {
@@ -307,14 +314,16 @@ typedef struct gx_serve_stats {
     uint64_t max_batch_jobs;  /* most jobs admitted into one pass */
     uint64_t jobs_waiting, jobs_running;
     uint64_t bytes_in_use;    /* estimated device bytes of the running jobs */
+    uint64_t jobs_cancelled;  /* withdrawn by gx_serve_cancel before they started */
 } gx_serve_stats;
 
 /* Start a server on ctx's device.  Each lane is a context of its own with one worker thread.
  * An idle lane admits, in arrival order, every waiting job whose estimated device memory
- * (from its input size) fits the budget next to the jobs already running, up to max_batch,
- * and runs them as one gx_batch_run pass; jobs that arrive meanwhile wait for the next free
- * lane, so batches form continuously and the lanes' passes overlap on the device.  The
- * oldest waiting job is always admitted when nothing runs.  Replaces submitting one
+ * (from its input size) fits the budget next to the jobs already running and the pass's
+ * pass_bytes, up to max_batch, and runs them as one gx_batch_run pass; jobs that arrive
+ * meanwhile wait for the next free lane, so batches form continuously and the lanes' passes
+ * overlap on the device.  The oldest waiting job is always admitted when nothing runs, and
+ * always opens the pass it is admitted to.  Replaces submitting one
  * GenomixHyracksDriver.runJob (GenomixHyracksDriver.java:84-135) per request; the
  * reference has no serving mode. */
 gx_status gx_serve_create(gx_ctx *ctx, const gx_serve_opts *opts, gx_server **out);
@@ -328,6 +337,12 @@ gx_status gx_serve_submit(gx_server *srv, gx_job *job, uint64_t *ticket);
  * submission to completion (the ticket is then released). */
 gx_status gx_serve_poll(gx_server *srv, uint64_t ticket, int timeout_ms, gx_status *job_status,
                         double *latency_ms);
+/* Withdraw a job that has not started yet: GX_OK, and the ticket's gx_serve_poll then reports
+ * GX_ECANCELLED; the job is the caller's again, unrun (destroy it, or submit it anew).
+ * GX_EBUSY when the job is already running (it completes as usual), GX_ESTATE when it is done,
+ * GX_EINVAL for an unknown ticket.  The reference has no counterpart: a Hyracks job is
+ * aborted as a whole (GenomixHyracksDriver.java:132-134). */
+gx_status gx_serve_cancel(gx_server *srv, uint64_t ticket);
 gx_status gx_serve_stats_get(gx_server *srv, gx_serve_stats *out);
 /* Runs every job still queued, then stops the lanes. */
 void gx_serve_destroy(gx_server *srv);

@@ -160,3 +160,32 @@ def test_oracle_parts_follow_the_reference_partitioner(parts):
             assert java_part(key[4:], parts) == q
             seen += 1
     assert seen == ref.nodes
+
+
+def test_jni_shim_compiles_against_the_header(tmp_path):
+    """The JNI side of the Java binding (genomix_gb300/jni/gxgpu_jni.c) compiles against
+    include/gxgpu.h.  No JDK is installed here, so a minimal jni.h with the types and the
+    JNIEnv functions the shim calls stands in for the real one."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    (tmp_path / "jni.h").write_text("""
+#include <stdint.h>
+typedef int32_t jint; typedef int64_t jlong; typedef void *jobject; typedef jobject jclass;
+typedef jobject jstring; typedef jobject jintArray; typedef int64_t jsize;
+struct JNINativeInterface_;
+typedef const struct JNINativeInterface_ *JNIEnv;
+struct JNINativeInterface_ {
+    void *(*GetDirectBufferAddress)(JNIEnv *, jobject);
+    void (*SetIntArrayRegion)(JNIEnv *, jintArray, jsize, jsize, const jint *);
+    jstring (*NewStringUTF)(JNIEnv *, const char *);
+    jobject (*NewDirectByteBuffer)(JNIEnv *, void *, jlong);
+};
+#define JNIEXPORT __attribute__((visibility("default")))
+#define JNICALL
+""")
+    src = os.path.join(ROOT, "genomix_gb300", "jni", "gxgpu_jni.c")
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-fsyntax-only", "-I", str(tmp_path), "-I",
+                    os.path.join(ROOT, "include"), src], check=True)

@@ -112,3 +112,77 @@ def test_destroy_runs_queued_jobs_and_oracle_parity(ctx):
         assert go.normalize(j.records()) == go.normalize(ref.records)
         j.close()
     assert len(tickets) == 4
+
+
+def test_cancel_a_queued_job(ctx):
+    """One lane busy with a large job; three small ones queue behind it and the middle one is
+    withdrawn: its poll reports GX_ECANCELLED, the job is unrun, and the others' records equal
+    their plain builds."""
+    big = synth.pe_5mbp(max_pairs=300_000)
+    works = mix(3, seed=19)
+    jbig = gx.GraphBuildJob(ctx, big.k)
+    jbig.add_input(big.text)
+    jobs = []
+    for w in works:
+        j = gx.GraphBuildJob(ctx, w.k)
+        j.add_input(w.text)
+        jobs.append(j)
+    with gx.Server(ctx, lanes=1) as srv:
+        tb = srv.submit(jbig)
+        tickets = [srv.submit(j) for j in jobs]
+        assert srv.cancel(tickets[1])
+        assert not srv.cancel(tickets[1])  # already withdrawn (done)
+        done = [srv.poll(t) for t in tickets]
+        assert srv.poll(tb)[0] == 0
+        st = srv.stats()
+        with pytest.raises(gx.GraphBuildError):
+            srv.cancel(123456789)  # unknown ticket
+    assert [s for s, _ in done] == [0, 11, 0]  # GX_ECANCELLED
+    assert st["jobs_cancelled"] == 1 and st["jobs_done"] == 3
+    for q in (0, 2):
+        assert go.normalize(jobs[q].records()) == go.normalize(alone(ctx, works[q]))
+    # the withdrawn job is the caller's again, unrun: it can still be built
+    jobs[1].run()
+    assert go.normalize(jobs[1].records()) == go.normalize(alone(ctx, works[1]))
+    for j in jobs + [jbig]:
+        j.close()
+
+
+def test_pass_cap_keeps_small_jobs_out_of_a_large_pass(ctx):
+    """A pass admits jobs up to pass_bytes of estimated device memory (its first job always):
+    with a cap below two jobs' estimate every pass holds one job."""
+    works = mix(6, seed=23)
+    done, recs, stats = serve_all(ctx, works, lanes=1, pass_bytes=1)
+    assert [st for st, _ in done] == [0] * len(works)
+    assert stats["batches"] == len(works) and stats["max_batch_jobs"] == 1
+    for w, rec in zip(works[:2], recs[:2]):
+        assert go.normalize(rec) == go.normalize(alone(ctx, w))
+
+
+def test_out_of_memory_batch_splits_in_halves():
+    """A context whose run allocations above a limit fail as out of memory (the testing option):
+    a batch whose buffers exceed it is split in halves until the pieces fit, and every job's
+    records still equal its plain build's."""
+    works = [synth.small_random(200 + i, 3000, 150, 31, paired=False, genome_len=40_000, err=0.005)
+             for i in range(8)]
+    limit = 12 * max(len(t) for t in works)  # one job's buffers fit, the whole batch's do not
+    refs = []
+    with gx.Context(0) as plain_ctx:
+        for t in works:
+            j = gx.GraphBuildJob(plain_ctx, 31)
+            j.add_input(t)
+            j.run()
+            refs.append(j.records())
+            j.close()
+    with gx.Context(0, test_alloc_fail_above=limit) as c:
+        jobs = []
+        for t in works:
+            j = gx.GraphBuildJob(c, 31)
+            j.add_input(t)
+            jobs.append(j)
+        assert gx.batch_run(c, jobs) == [0] * len(works)
+        passes = {j.stats()["ms_total"] for j in jobs}
+        assert len(passes) > 1  # not one pass
+        for j, ref in zip(jobs, refs):
+            assert go.normalize(j.records()) == go.normalize(ref)
+            j.close()
