@@ -7,7 +7,8 @@
 // else is in flight, so a job larger than the budget still runs, alone), up to `max_batch`
 // jobs, and runs them as one gx_batch_run pass.  Every job of a pass finishes when the pass
 // does, so the cap keeps small jobs out of a large job's pass: the large one runs on a lane of
-// its own while the other lanes keep serving the small ones.  Jobs that arrive while lanes
+// its own while the other lanes keep serving the small ones, and large jobs (above a quarter
+// of the cap) never hold every lane at once.  Jobs that arrive while lanes
 // are busy are picked up by the next lane to free up: batches form continuously, and the
 // passes of different lanes overlap on the device.  Results stay device-resident in their jobs until the caller emits and destroys
 // them.  While the server runs a job, the job belongs to it: call nothing on that job until
@@ -50,6 +51,7 @@ struct Ticket {
     gx_job *job = nullptr;
     gx_ctx *home = nullptr;
     size_t est = 0;
+    bool large = false;  // estimated above a quarter of pass_bytes
     double t_submit = 0, t_start = 0, t_done = 0;
     gx_status st = GX_OK;
     bool done = false;
@@ -69,6 +71,7 @@ struct gx_server {
     size_t budget = 0, in_use = 0, pass_bytes = 0;
     int max_batch = 64;
     int running = 0;
+    int large_passes = 0;  // passes in flight that hold a large job
     bool stop = false;
     gx_serve_stats stats{};
 };
@@ -90,25 +93,39 @@ static void lane_loop_impl(gx_server *sv, gx_ctx *lane) {
     std::unique_lock<std::mutex> lk(sv->mu);
     for (;;) {
         // admit in arrival order while memory lasts
+        // Large jobs hold at most lanes - 1 lanes: while they do, an idle lane passes over them
+        // (they keep their order among themselves) and admits the small jobs behind them.
         std::vector<uint64_t> take;
+        std::vector<size_t> take_pos;
         size_t est = 0;
+        bool large = false;
+        const int lanes = (int)sv->lanes.size();
         for (;;) {
             take.clear();
+            take_pos.clear();
             est = 0;
-            for (uint64_t id : sv->pending) {
+            large = false;
+            size_t pos = 0;
+            for (auto it = sv->pending.begin(); it != sv->pending.end(); ++it, ++pos) {
+                const uint64_t id = *it;
                 if ((int)take.size() >= sv->max_batch) break;
-                const size_t e = sv->tickets[id].est;
+                const Ticket &t = sv->tickets[id];
+                if (t.large && lanes > 1 && sv->large_passes >= lanes - 1) continue;
+                const size_t e = t.est;
                 const bool alone = take.empty() && sv->in_use == 0;
                 if (!alone && sv->in_use + est + e > sv->budget) break;  // keep arrival order
                 if (!take.empty() && est + e > sv->pass_bytes) break;   // the pass is full
                 take.push_back(id);
+                take_pos.push_back(pos);
                 est += e;
+                large = large || t.large;
             }
             if (!take.empty() || (sv->stop && sv->pending.empty())) break;
             sv->cv_work.wait(lk);
         }
         if (take.empty()) return;  // stopping, nothing left
-        for (size_t q = 0; q < take.size(); q++) sv->pending.pop_front();
+        for (size_t q = take_pos.size(); q-- > 0;) sv->pending.erase(sv->pending.begin() + (long)take_pos[q]);
+        if (large) sv->large_passes++;
         sv->in_use += est;
         sv->running += (int)take.size();
         std::vector<gx_job *> jobs;
@@ -134,6 +151,7 @@ static void lane_loop_impl(gx_server *sv, gx_ctx *lane) {
             t.done = true;
         }
         sv->in_use -= est;
+        if (large) sv->large_passes--;
         sv->running -= (int)take.size();
         sv->stats.jobs_done += take.size();
         sv->cv_done.notify_all();
@@ -201,6 +219,7 @@ static gx_status serve_submit_impl(gx_server *sv, gx_job *j, uint64_t *ticket) {
     t.job = j;
     t.home = j->ctx;
     t.est = estimate_bytes(j);
+    t.large = t.est > sv->pass_bytes / 4;
     t.t_submit = now_ms();
     sv->tickets[id] = t;
     sv->pending.push_back(id);

@@ -323,7 +323,9 @@ typedef struct gx_serve_stats {
  * pass_bytes, up to max_batch, and runs them as one gx_batch_run pass; jobs that arrive
  * meanwhile wait for the next free lane, so batches form continuously and the lanes' passes
  * overlap on the device.  The oldest waiting job is always admitted when nothing runs, and
- * always opens the pass it is admitted to.  Replaces submitting one
+ * always opens the pass it is admitted to.  Large jobs (estimated above a quarter of
+ * pass_bytes) hold at most lanes - 1 lanes at a time, so small jobs always find a lane; while
+ * they do, an idle lane passes over the large jobs waiting.  Replaces submitting one
  * GenomixHyracksDriver.runJob (GenomixHyracksDriver.java:84-135) per request; the
  * reference has no serving mode. */
 gx_status gx_serve_create(gx_ctx *ctx, const gx_serve_opts *opts, gx_server **out);
