@@ -1653,6 +1653,16 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
     } else {
         w.empty();
     }
+    // The super buckets this CTA can reach: its reads lie in a run of consecutive samples, which
+    // own a contiguous range of buckets (a plain job: all of them).  The per-round loops below
+    // cover that range only, so a batch of many samples pays for its own samples' buckets.
+    uint32_t lo = 0, hi = S;
+    if (m.n > 1) {
+        const uint32_t ra = blockIdx.x * SC_THREADS, rb = min(n_reads, ra + SC_THREADS) - 1;
+        const SamplePlan pa = m.plan[sample_of_read(m, ra)], pb = m.plan[sample_of_read(m, rb)];
+        lo = pa.super_base;
+        hi = pb.super_base + (1u << pb.log_s);
+    }
     if (threadIdx.x == 0) sm.rounds = 0;
     if (hll)
         for (uint32_t i = threadIdx.x; i < SC_HLL_REGS; i += blockDim.x) sm.hll[i] = 0;
@@ -1663,7 +1673,7 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
     K ck[CACHE ? RN : 1];
     uint32_t cb[CACHE ? RN : 1];  // edge bits | super << 16
     for (uint32_t round = 0; round < rounds; round++) {
-        for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) sm_cur[i] = 0;
+        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) sm_cur[i] = 0;
         __syncthreads();
         const Walker<K> w0 = w;
         const uint32_t nq = w.j < w.nk ? min((uint32_t)RN, w.nk - w.j) : 0u;
@@ -1688,7 +1698,7 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
             }
         }
         __syncthreads();
-        for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) {
+        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
             const uint32_t c = sm_cur[i];
             sm_loff[i] = c;
             uint32_t g = c ? atomicAdd(&s_cur[i], c) : 0u;
@@ -1699,10 +1709,10 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
             sm_gbase[i] = g;
         }
         __syncthreads();
-        const uint32_t tot = block_scan_array(sm_loff, S, sm.ws);
+        const uint32_t tot = block_scan_array(sm_loff + lo, hi - lo, sm.ws);
         // element i of bucket sp goes to s_off[sp] + gbase[sp] + (i - loff[sp]): the base, as
         // gbase (high word, ~0 for a bucket out of room) and glo (low word)
-        for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) {
+        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
             sm_cur[i] = 0;
             const uint32_t g = sm_gbase[i];
             if (g != 0xffffffffu) {
