@@ -226,7 +226,7 @@ def serving_workload(n_pool=48):
 
 
 SERVE_RATES = (25, 50, 100, 200, 400, 800)  # offered jobs/s
-SERVE_REQUESTS = 96                         # requests per rate, cycling through the job pool
+SERVE_REQUESTS = 192                        # requests per rate, cycling through the job pool
 SERVE_CLIENTS = 4                           # client threads submitting the arrivals
 
 
