@@ -470,7 +470,14 @@ def compact_tune(t):
     """The autotuner's choice without its per-candidate list (that goes to --details)."""
     if not t:
         return t
-    return {k: t[k] for k in ("algorithm", "load_factor", "ms") if k in t} | {"tried": len(t.get("candidates", []))}
+    out = {k: t[k] for k in ("algorithm", "load_factor", "threads_per_read", "ms") if k in t}
+    # the fastest of each tiling, so the line shows what the tiling dimension is worth
+    best = {}
+    for c in t.get("candidates", []):
+        if c["algorithm"] == "partitioned" and c["ms"] >= 0:
+            tp = c["threads_per_read"]
+            best[tp] = min(best.get(tp, c["ms"]), c["ms"])
+    return out | {"tried": len(t.get("candidates", [])), "best_ms_by_threads_per_read": best}
 
 
 def compact_serving(srv):

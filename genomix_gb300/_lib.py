@@ -108,12 +108,14 @@ class GraphStats(ctypes.Structure):
 
 
 class TuneCand(ctypes.Structure):
-    _fields_ = [("algorithm", ctypes.c_int), ("load_factor", ctypes.c_double), ("ms", ctypes.c_double)]
+    _fields_ = [("algorithm", ctypes.c_int), ("load_factor", ctypes.c_double), ("ms", ctypes.c_double),
+                ("threads_per_read", ctypes.c_int)]
 
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_size_t), ("algorithm", ctypes.c_int), ("load_factor", ctypes.c_double),
-                ("ms", ctypes.c_double), ("tried", ctypes.c_int), ("cand", TuneCand * 16)]
+                ("ms", ctypes.c_double), ("tried", ctypes.c_int), ("threads_per_read", ctypes.c_int),
+                ("cand", TuneCand * 16)]
 
 
 class Digest(ctypes.Structure):

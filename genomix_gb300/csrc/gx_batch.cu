@@ -290,7 +290,7 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         const SampleMap smap{read_base, d_plan, n};
         CK(cudaEventRecord(tm.ev[2], s));
         launch_scatter_super(wide, text, n_text, lines, reads, n_reads, k, smap, S, d_soff, s_cur, okey, obits,
-                             0xffffffffu, nullptr, nullptr, s);
+                             0xffffffffu, nullptr, nullptr, s, (uint32_t)jobs[0]->eff_threads_per_read);
         launch_heads_part(wide, text, n_text, lines, reads, n_reads, k, smap, heads, head_cnt, s);
         exclusive_scan_u32(head_cnt, head_off, P, nullptr, pscratch, s);
         launch_head_scatter_part(heads, reads, lines, n_reads, head_off, head_cur, head_idx, hsorted, s);
@@ -464,7 +464,7 @@ static gx_status batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses)
     cudaSetDevice(c->device);
     const AllocLimitScope als(c->test_alloc_fail_above);
     std::map<gx_job *, gx_status> result;
-    std::map<int, std::vector<gx_job *>> by_k;
+    std::map<long long, std::vector<gx_job *>> by_k;
     for (int i = 0; i < n; i++) {
         gx_job *j = jobs[i];
         if (!j || j->ctx != c) continue;
@@ -484,7 +484,8 @@ static gx_status batch_run(gx_ctx *c, gx_job **jobs, int n, gx_status *statuses)
             result[j] = pe;
             continue;
         }
-        by_k[j->k * 4096 + (int)(j->eff_load_factor * 1000)].push_back(j);  // same k and fill
+        // one pass per k, fill and tiling
+        by_k[((long long)j->k * 4096 + (int)(j->eff_load_factor * 1000)) * 64 + j->eff_threads_per_read].push_back(j);
         result[j] = GX_OK;  // placeholder until its group runs
     }
     for (auto &kv : by_k) {

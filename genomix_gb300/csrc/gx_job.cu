@@ -201,6 +201,10 @@ static gx_status job_create_impl(gx_ctx *c, const gx_job_opts *opts, gx_job **ou
     if (opts->input_kind != GX_INPUT_READID && opts->input_kind != GX_INPUT_FASTQ) return GX_EINVAL;
     if (opts->out_parts < 0 || opts->load_factor < 0 || opts->load_factor > 0.95) return GX_EINVAL;
     if (opts->max_readids_per_edge < 0) return GX_EINVAL;  // GenomixJobConf.validateConf :456-457
+    {
+        const int t = opts->threads_per_read;
+        if (t < 0 || t > 32 || (t & (t - 1))) return GX_EINVAL;  // 0 or a power of two up to 32
+    }
     const bool has_plan = opts->struct_size >= offsetof(gx_job_opts, plan) + sizeof(int);
     if (has_plan && opts->plan != GX_PLAN_BUILD_DEBRUIJN_GRAPH && opts->plan != GX_PLAN_BUILD_READ_PARSER)
         return GX_EINVAL;
@@ -952,7 +956,7 @@ static gx_status build_partitioned(RunCtx &rc) {
             CK(cudaMemcpyAsync(d_plan, &hp, sizeof hp, cudaMemcpyHostToDevice, s));
             CK(cudaMemcpyAsync(d_soff, soff.data(), (S + 1) * 8ull, cudaMemcpyHostToDevice, s));
             launch_scatter_super(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, S, d_soff, s_cur,
-                                 okey, obits, (uint32_t)cap, d_hll, d_ovf, s);
+                                 okey, obits, (uint32_t)cap, d_hll, d_ovf, s, (uint32_t)j->eff_threads_per_read);
             std::vector<uint32_t> hh(SC_HLL_REGS);
             uint32_t ovf = 0;
             CK(d2h_async(scount.data(), s_cur, S * 4ull, s));
@@ -1034,7 +1038,7 @@ static gx_status build_partitioned(RunCtx &rc) {
         if (counted) {
             // A2 into the counted offsets
             launch_scatter_super(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, S, d_soff, s_cur,
-                                 okey, obits, 0xffffffffu, nullptr, nullptr, s);
+                                 okey, obits, 0xffffffffu, nullptr, nullptr, s, (uint32_t)j->eff_threads_per_read);
         }
         // read heads
         launch_heads_part(wide, rc.text, rc.n_text, rc.lines, rc.reads, n_reads, k, smap, heads, head_cnt, s);
@@ -1324,11 +1328,13 @@ static gx_status run_job(gx_job *j) {
 void gxi::resolve_options(gx_job *j) {
     j->eff_algorithm = j->o.algorithm == GX_ALGO_TABLE ? GX_ALGO_TABLE : GX_ALGO_PARTITIONED;
     j->eff_load_factor = j->o.load_factor;
+    j->eff_threads_per_read = j->o.threads_per_read > 0 ? j->o.threads_per_read : 1;
     const gx_ctx::Tuned &t = j->ctx->tuned[j->wide];
     if (j->o.algorithm == GX_ALGO_DEFAULT && j->o.load_factor == 0 && t.valid) {
         j->eff_algorithm = t.algorithm;
         j->eff_load_factor = t.load_factor;
     }
+    if (j->o.threads_per_read == 0 && t.valid) j->eff_threads_per_read = t.threads_per_read;
 }
 
 double gxi::bucket_target(double load_factor) {

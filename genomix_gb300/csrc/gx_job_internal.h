@@ -56,6 +56,7 @@ struct gx_ctx {
         bool valid = false;
         int algorithm = GX_ALGO_PARTITIONED;
         double load_factor = 0;
+        int threads_per_read = 1;
     } tuned[2];
 };
 
@@ -87,6 +88,7 @@ struct gx_job {
     // the algorithm and fill this run uses: the job's options, or the context's tuned choice
     int eff_algorithm = GX_ALGO_PARTITIONED;
     double eff_load_factor = 0;
+    int eff_threads_per_read = 1;
     // a batched run writes every sample's records into one buffer: the jobs share ownership
     std::shared_ptr<void> out_owner;
 };
@@ -156,8 +158,8 @@ gx_status guarded(const char *where, F &&f) {
     }
 }
 
-// The algorithm and fill a job runs with: its own options where set, else the context's
-// tuned choice for its key width, else the built-in defaults.
+// The algorithm, fill and threads per read a job runs with: its own options where set, else the
+// context's tuned choice for its key width, else the built-in defaults.
 void resolve_options(gx_job *j);
 // Fine-bucket fill aimed for by the partitioned build (distinct k-mers per 2048-slot table).
 double bucket_target(double load_factor);

@@ -1303,7 +1303,7 @@ struct Walker {
     unsigned long long n_text, xo;  // next unread letter offset
     unsigned long long xbuf;
     uint32_t xn;
-    uint32_t nk, j, yb;
+    uint32_t nk, j, jend, yb;  // occurrences of the read; the walk's next and end
     int k, sh;
     K mask, fwd, rc;
     uint32_t d, pd;
@@ -1327,16 +1327,32 @@ struct Walker {
     }
     __device__ __forceinline__ void init(const uint8_t *text_, unsigned long long n_text_, unsigned long long s_off,
                                          uint32_t L, int k_) {
+        init_range(text_, n_text_, s_off, L, k_, 0, L - (uint32_t)k_ + 1);
+    }
+    // Occurrences [jb, je) of a read only (one segment of a read split over several threads).
+    // A segment after the first starts one k-mer early and steps over it, so its first
+    // occurrence gets the edge bits from its predecessor exactly as a whole-read walk does;
+    // whether an occurrence has a successor is judged by the read's own length.
+    __device__ __forceinline__ void init_range(const uint8_t *text_, unsigned long long n_text_,
+                                               unsigned long long s_off, uint32_t L, int k_, uint32_t jb, uint32_t je) {
         text = text_;
         n_text = n_text_;
-        xo = s_off;
+        k = k_;
+        nk = L - (uint32_t)k + 1;
+        if (je > nk) je = nk;
+        if (jb >= je) {
+            j = jend = 0;
+            return;
+        }
+        const uint32_t j0 = jb ? jb - 1 : 0;
+        xo = s_off + j0;
         xn = 0;
         xbuf = 0;
-        // the read's sectors requested up front: the walk then consumes them from L1 instead of
-        // waiting on one 8-byte load after another
-        for (unsigned long long a = s_off & ~31ULL; a < s_off + L && a < n_text; a += 32)
+        // the segment's sectors requested up front: the walk then consumes them from L1 instead
+        // of waiting on one 8-byte load after another
+        const unsigned long long seg_end = s_off + je + (uint32_t)k - 1;
+        for (unsigned long long a = xo & ~31ULL; a < seg_end && a < n_text; a += 32)
             asm volatile("prefetch.global.L1 [%0];" ::"l"(text + a));
-        k = k_;
         sh = 2 * (k - 1);
         mask = KeyOps<K>::mask(k);
         fwd = 0;
@@ -1346,17 +1362,22 @@ struct Walker {
             fwd = (fwd >> 2) | ((K)c << sh);
             rc = ((rc << 2) | (K)(3u - c)) & mask;
         }
-        nk = L - (uint32_t)k + 1;
-        j = 0;
+        j = j0;
+        jend = je;
         d = fwd <= rc ? 0u : 1u;
         pd = 0;
         yb = 0;
+        if (jb) {  // occurrence jb - 1: its direction and first letter carry over
+            K c;
+            uint32_t b, dd;
+            next(c, b, dd);
+        }
     }
     __device__ __forceinline__ void empty() {
         nk = 0;
-        j = 0;
+        j = jend = 0;
     }
-    __device__ __forceinline__ bool done() const { return j >= nk; }
+    __device__ __forceinline__ bool done() const { return j >= jend; }
     // the current occurrence: canonical value, its <= 2 edge bits, orientation; then advance
     __device__ __forceinline__ void next(K &canon, uint32_t &bits, uint32_t &dir) {
         const bool hn = j + 1 < nk;
@@ -1389,6 +1410,19 @@ __device__ __forceinline__ void walker_for(Walker<K> &w, const uint8_t *text, un
     const LineRec lr = lines[rl >> 1];
     const uint32_t mate = rl & 1u;
     w.init(text, n_text, mate ? lr.s1 : lr.s0, mate ? lr.l1 : lr.l0, k);
+}
+
+// Segment `seg` of `tpr` near-equal segments of read r's occurrences.
+template <class K>
+__device__ __forceinline__ void walker_for_seg(Walker<K> &w, const uint8_t *text, unsigned long long n_text,
+                                               const LineRec *lines, const uint32_t *reads, uint32_t r, int k,
+                                               uint32_t seg, uint32_t tpr) {
+    const uint32_t rl = reads[r];
+    const LineRec lr = lines[rl >> 1];
+    const uint32_t mate = rl & 1u;
+    const uint32_t L = mate ? lr.l1 : lr.l0, nk = L - (uint32_t)k + 1;
+    const uint32_t per = (nk + tpr - 1) / tpr;
+    w.init_range(text, n_text, mate ? lr.s1 : lr.s0, L, k, seg * per, seg * per + per);
 }
 
 __device__ __forceinline__ uint32_t super_of(uint64_t h, uint32_t log_s) { return (uint32_t)(h >> (64 - log_s)); }
@@ -1635,18 +1669,25 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
                                                               SampleMap m, uint32_t S,
                                                               const unsigned long long *s_off,
                                                               uint32_t *s_cur, K *okey, uint16_t *obits,
-                                                              uint32_t cap, uint32_t *hll, uint32_t *ovf) {
+                                                              uint32_t cap, uint32_t *hll, uint32_t *ovf,
+                                                              uint32_t tpr) {
     constexpr bool CACHE = SuperRound<K>::CACHE;
     constexpr int RN = SuperRound<K>::N;
     extern __shared__ __align__(16) uint8_t smem_raw[];
     SuperSmem<K> &sm = *reinterpret_cast<SuperSmem<K> *>(smem_raw);
     uint32_t *const sm_loff = sm.arrays, *const sm_gbase = sm.arrays + S, *const sm_cur = sm.arrays + 2 * S;
     uint32_t *const sm_glo = sm.arrays + 3 * S;
-    const uint32_t r = blockIdx.x * SC_THREADS + threadIdx.x;
+    // tpr threads per read (a power of two up to 32): thread t walks segment t % tpr of read
+    // t / tpr, so a read's occurrences are spread over tpr threads of one warp
+    const uint32_t lg_tpr = 31 - __clz(tpr), per_cta = SC_THREADS >> lg_tpr;
+    const uint32_t r = blockIdx.x * per_cta + (threadIdx.x >> lg_tpr);
     Walker<K> w;
     uint32_t sbase = 0, log_s = 0;
     if (r < n_reads) {
-        walker_for(w, text, n_text, lines, reads, r, k);
+        if (tpr == 1)
+            walker_for(w, text, n_text, lines, reads, r, k);
+        else
+            walker_for_seg(w, text, n_text, lines, reads, r, k, threadIdx.x & (tpr - 1), tpr);
         const SamplePlan pl = m.plan[sample_of_read(m, r)];
         sbase = pl.super_base;
         log_s = pl.log_s;
@@ -1658,7 +1699,7 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
     // cover that range only, so a batch of many samples pays for its own samples' buckets.
     uint32_t lo = 0, hi = S;
     if (m.n > 1) {
-        const uint32_t ra = blockIdx.x * SC_THREADS, rb = min(n_reads, ra + SC_THREADS) - 1;
+        const uint32_t ra = blockIdx.x * per_cta, rb = min(n_reads, ra + per_cta) - 1;
         const SamplePlan pa = m.plan[sample_of_read(m, ra)], pb = m.plan[sample_of_read(m, rb)];
         lo = pa.super_base;
         hi = pb.super_base + (1u << pb.log_s);
@@ -1667,7 +1708,7 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
     if (hll)
         for (uint32_t i = threadIdx.x; i < SC_HLL_REGS; i += blockDim.x) sm.hll[i] = 0;
     __syncthreads();
-    atomicMax(&sm.rounds, (w.nk + RN - 1) / RN);
+    atomicMax(&sm.rounds, (w.jend - w.j + RN - 1) / RN);
     __syncthreads();
     const uint32_t rounds = sm.rounds;
     K ck[CACHE ? RN : 1];
@@ -1676,7 +1717,7 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
         for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) sm_cur[i] = 0;
         __syncthreads();
         const Walker<K> w0 = w;
-        const uint32_t nq = w.j < w.nk ? min((uint32_t)RN, w.nk - w.j) : 0u;
+        const uint32_t nq = w.j < w.jend ? min((uint32_t)RN, w.jend - w.j) : 0u;
         // count this round's occurrences per super bucket
 #pragma unroll
         for (int q = 0; q < RN; q++) {
@@ -1762,21 +1803,22 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
 void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
                           const uint32_t *reads, uint32_t n_reads, int k, SampleMap m, uint32_t n_super,
                           const unsigned long long *s_off, uint32_t *s_cur, void *okey, uint16_t *obits,
-                          uint32_t cap, uint32_t *hll, uint32_t *ovf, cudaStream_t s) {
+                          uint32_t cap, uint32_t *hll, uint32_t *ovf, cudaStream_t s, uint32_t tpr) {
     if (!n_reads) return;
-    const unsigned blocks = (n_reads + SC_THREADS - 1) / SC_THREADS;
+    if (tpr < 1 || tpr > 32 || (tpr & (tpr - 1))) tpr = 1;
+    const unsigned blocks = (unsigned)(((uint64_t)n_reads * tpr + SC_THREADS - 1) / SC_THREADS);
     t_launches++;
     if (wide) {
         const size_t sm = SuperSmem<u128>::bytes(n_super);
         cudaFuncSetAttribute(k_scatter_super<u128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_scatter_super<u128><<<blocks, SC_THREADS, sm, s>>>(text, n_text, lines, reads, n_reads, k, m, n_super,
-                                                             s_off, s_cur, (u128 *)okey, obits, cap, hll, ovf);
+                                                             s_off, s_cur, (u128 *)okey, obits, cap, hll, ovf, tpr);
     } else {
         const size_t sm = SuperSmem<uint64_t>::bytes(n_super);
         cudaFuncSetAttribute(k_scatter_super<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_scatter_super<uint64_t><<<blocks, SC_THREADS, sm, s>>>(text, n_text, lines, reads, n_reads, k, m,
                                                                  n_super, s_off, s_cur, (uint64_t *)okey, obits, cap,
-                                                                 hll, ovf);
+                                                                 hll, ovf, tpr);
     }
 }
 

@@ -160,7 +160,7 @@ void launch_sample_bounds(const unsigned long long *text_base, uint32_t n_sample
 void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
                           const uint32_t *reads, uint32_t n_reads, int k, SampleMap m, uint32_t n_super,
                           const unsigned long long *s_off, uint32_t *s_cur, void *okey, uint16_t *obits,
-                          uint32_t cap, uint32_t *hll, uint32_t *ovf, cudaStream_t s);
+                          uint32_t cap, uint32_t *hll, uint32_t *ovf, cudaStream_t s, uint32_t tpr = 1);
 // chunks: (start, super << 32 | length) of CHUNK-sized pieces of each super bucket
 void launch_make_chunks(const unsigned long long *soff, const uint32_t *scount, const uint32_t *cbase, uint32_t S,
                         ulonglong2 *chunks, cudaStream_t s);

@@ -1,10 +1,13 @@
 // gx_tune.cu — the autotuner (gx_autotune).
 //
-// Times each candidate (aggregation algorithm x table fill) on a sample of the caller's reads
-// and keeps the fastest in the context, per key width: jobs created with the default
-// algorithm and load factor then run with it (plain, batched and served alike).  The best fill
-// depends on the data: more distinct k-mers per bucket means fewer buckets and less
-// per-bucket work, up to the point where probing and overflow retries cost more.
+// Times each candidate (aggregation algorithm x table fill x threads per read) on a sample of
+// the caller's reads and keeps the fastest in the context, per key width: jobs created with
+// the default algorithm, load factor and tiling then run with it (plain, batched and served
+// alike).  The best fill (the partitioned build's bucket width: distinct k-mers per bucket
+// table) depends on the data: more per bucket means fewer buckets and less per-bucket work, up
+// to the point where probing and overflow retries cost more.  The tiling splits each read's
+// k-mer walk over 1, 2 or 4 threads: shorter walks per thread and a smaller text footprint per
+// CTA, against one extra k-mer window per segment.
 #include <algorithm>
 #include <cstdio>
 #include <mutex>
@@ -19,13 +22,17 @@ namespace {
 struct Candidate {
     int algorithm;
     double load_factor;
+    int threads_per_read;
 };
 
 const Candidate kCandidates[] = {
-    {GX_ALGO_PARTITIONED, 0.30}, {GX_ALGO_PARTITIONED, 0.35}, {GX_ALGO_PARTITIONED, 0.4375},
-    {GX_ALGO_PARTITIONED, 0.50}, {GX_ALGO_PARTITIONED, 0.60}, {GX_ALGO_TABLE, 0.35},
-    {GX_ALGO_TABLE, 0.50},       {GX_ALGO_TABLE, 0.70},
+    {GX_ALGO_PARTITIONED, 0.35, 1},   {GX_ALGO_PARTITIONED, 0.4375, 1}, {GX_ALGO_PARTITIONED, 0.50, 1},
+    {GX_ALGO_PARTITIONED, 0.60, 1},   {GX_ALGO_PARTITIONED, 0.35, 2},   {GX_ALGO_PARTITIONED, 0.4375, 2},
+    {GX_ALGO_PARTITIONED, 0.50, 2},   {GX_ALGO_PARTITIONED, 0.60, 2},   {GX_ALGO_PARTITIONED, 0.35, 4},
+    {GX_ALGO_PARTITIONED, 0.4375, 4}, {GX_ALGO_PARTITIONED, 0.50, 4},   {GX_ALGO_PARTITIONED, 0.60, 4},
+    {GX_ALGO_TABLE, 0.35, 1},         {GX_ALGO_TABLE, 0.50, 1},         {GX_ALGO_TABLE, 0.70, 1},
 };
+static_assert(sizeof kCandidates / sizeof kCandidates[0] <= GX_TUNE_MAX, "gx_tune_result holds every candidate");
 
 // device time of one build of the sample with the given settings (< 0: the build failed)
 double time_one(gx_ctx *c, const void *d_text, size_t bytes, int k, const Candidate &cd, gx_status &st) {
@@ -36,6 +43,7 @@ double time_one(gx_ctx *c, const void *d_text, size_t bytes, int k, const Candid
     o.out_parts = 1;
     o.algorithm = cd.algorithm;
     o.load_factor = cd.load_factor;
+    o.threads_per_read = cd.threads_per_read;
     gx_job *j = nullptr;
     if ((st = gx_job_create(c, &o, &j)) != GX_OK) return -1;
     double ms = -1;
@@ -90,6 +98,7 @@ extern "C" gx_status gx_autotune(gx_ctx *c, const void *sample, size_t bytes, in
             }
             out->cand[i].algorithm = kCandidates[i].algorithm;
             out->cand[i].load_factor = kCandidates[i].load_factor;
+            out->cand[i].threads_per_read = kCandidates[i].threads_per_read;
             out->cand[i].ms = t;
             out->tried++;
             if (t >= 0 && (best < 0 || t < out->cand[best].ms)) best = i;
@@ -103,12 +112,14 @@ extern "C" gx_status gx_autotune(gx_ctx *c, const void *sample, size_t bytes, in
         if (best < 0) return first_err != GX_OK ? first_err : GX_ECUDA;
         out->algorithm = kCandidates[best].algorithm;
         out->load_factor = kCandidates[best].load_factor;
+        out->threads_per_read = kCandidates[best].threads_per_read;
         out->ms = out->cand[best].ms;
         std::lock_guard<std::mutex> lk(c->mu);
         gx_ctx::Tuned &tu = c->tuned[k > 32 ? 1 : 0];
         tu.valid = true;
         tu.algorithm = out->algorithm;
         tu.load_factor = out->load_factor;
+        tu.threads_per_read = out->threads_per_read;
         return GX_OK;
     });
 }

@@ -107,8 +107,9 @@ class Context:
         return ms.value
 
     def autotune(self, sample, k, repeats=2):
-        """gx_autotune: times every algorithm x fill on `sample` (readid text) and keeps the
-        fastest for jobs at the defaults; returns the choice and every candidate's time."""
+        """gx_autotune: times every algorithm x fill x threads-per-read on `sample` (readid text)
+        and keeps the fastest for jobs at the defaults; returns the choice and every candidate's
+        time."""
         r = _lib.TuneResult()
         r.struct_size = ctypes.sizeof(_lib.TuneResult)
         p, n, keep = _host_ptr(sample)
@@ -116,8 +117,10 @@ class Context:
         del keep
         names = {_lib.ALGO_PARTITIONED: "partitioned", _lib.ALGO_TABLE: "table"}
         return {"algorithm": names[r.algorithm], "load_factor": r.load_factor, "ms": r.ms,
+                "threads_per_read": r.threads_per_read,
                 "candidates": [{"algorithm": names[r.cand[i].algorithm], "load_factor": r.cand[i].load_factor,
-                                "ms": r.cand[i].ms} for i in range(r.tried)]}
+                                "threads_per_read": r.cand[i].threads_per_read, "ms": r.cand[i].ms}
+                               for i in range(r.tried)]}
 
     def autotune_clear(self):
         _check(self._L.gx_autotune_clear(self.h), "gx_autotune_clear")

@@ -93,7 +93,9 @@ typedef struct gx_job_opts {
                                  else the built-in default (table build: slots = occurrences / 0.5;
                                  partitioned build: 896 of 2048 per bucket) */
     int max_readids_per_edge; /* accepted and ignored, as in the reference (GenomixJobConf.java:718) */
-    int threads_per_read;     /* reserved: every k-mer walk runs one thread per read */
+    int threads_per_read;     /* threads that walk one read in the partitioned build's occurrence scatter,
+                                 each a contiguous segment of its k-mers: 1, 2, 4, 8, 16 or 32;
+                                 0 = the context's autotuned choice, else 1 */
     size_t est_input_bytes;   /* capacity hint for the device input buffer; 0 = grow on demand */
     int algorithm;            /* GX_ALGO_*: how occurrences are aggregated */
     int plan;                 /* GX_PLAN_*: what the job writes */
@@ -275,20 +277,24 @@ gx_status gx_job_graph_stats(gx_job *job, gx_graph_stats *out);
 typedef struct gx_tune_result {
     size_t struct_size;  /* sizeof(gx_tune_result), set by the caller */
     int algorithm;       /* the fastest: GX_ALGO_PARTITIONED or GX_ALGO_TABLE */
-    double load_factor;  /* and its fill (partitioned: distinct k-mers per 2048-slot bucket table) */
+    double load_factor;  /* and its fill: the bucket width of the partitioned build (distinct
+                            k-mers per 2048-slot bucket table), the table build's load factor */
     double ms;           /* its device time on the sample */
     int tried;
+    int threads_per_read;  /* and its tiling of the k-mer walk (partitioned build) */
     struct {
         int algorithm;
         double load_factor;
         double ms;       /* best of the repeats; < 0 if the candidate failed */
+        int threads_per_read;
     } cand[GX_TUNE_MAX];
 } gx_tune_result;
 
-/* Time every candidate (algorithm x fill) on `sample` (readid text in host memory, e.g. the
+/* Time every candidate (algorithm x fill x threads per read) on `sample` (readid text in host memory, e.g. the
  * first tens of MB of a run's input) `repeats` times (0 = 2) and keep the fastest in the
  * context for k-mers of k's key width (64-bit for k <= 32, 128-bit above): jobs created with
- * GX_ALGO_DEFAULT and load_factor 0 then use it, in gx_job_run, gx_batch_run and serving.
+ * GX_ALGO_DEFAULT, load_factor 0 and threads_per_read 0 then use it, in gx_job_run,
+ * gx_batch_run and serving.
  * The reference has no counterpart (its sort-based aggregation has no such parameters). */
 gx_status gx_autotune(gx_ctx *ctx, const void *sample, size_t bytes, int k, int repeats, gx_tune_result *out);
 /* Forget the tuned choices: jobs at the defaults use the built-in settings again. */

@@ -65,6 +65,29 @@ def test_random_single_end_all_k(ctx, k, algo):
     assert_same(ctx, text, k, algorithm=algo)
 
 
+@pytest.mark.parametrize("tpr", [2, 4, 32])
+@pytest.mark.parametrize("k", [3, 4, 5, 8, 15, 16, 21, 31, 32, 33, 36, 47, 55, 63, 64])
+def test_split_read_walk_all_k(ctx, k, tpr):
+    """The partitioned build with each read's k-mer walk split over tpr threads (segments of
+    its occurrences, edge bits carried across the cuts): the oracle's records for every k,
+    including reads shorter than the number of segments."""
+    text = synth.small_random(300 + k, 300, max(k + 20, 70), k, genome_len=1500, err=0.02)
+    assert_same(ctx, text, k, algorithm="partitioned", threads_per_read=tpr)
+
+
+@pytest.mark.parametrize("tpr", [2, 4, 8])
+@pytest.mark.parametrize("k", [21, 31, 55])
+def test_split_read_walk_paired(ctx, k, tpr):
+    text = synth.small_random(400 + k, 400, 150, k, paired=True, genome_len=5000, err=0.01, n_rate=0.003)
+    assert_same(ctx, text, k, algorithm="partitioned", threads_per_read=tpr)
+
+
+def test_threads_per_read_must_be_a_power_of_two(ctx):
+    for bad in (3, 6, 64, -1):
+        with pytest.raises(gx.GraphBuildError):
+            gx.GraphBuildJob(ctx, 31, threads_per_read=bad)
+
+
 @pytest.mark.parametrize("algo", ALGOS)
 @pytest.mark.parametrize("k", [21, 31, 55])
 def test_random_paired_with_n(ctx, k, algo):
