@@ -1642,12 +1642,19 @@ void launch_sample_bounds(const unsigned long long *text_base, uint32_t n_sample
 }
 
 // ---- A2 -------------------------------------------------------------------------------------
-// shared layout of k_scatter_super: staging for one round, then three S-entry arrays
+// A round's k-mers stay in registers between counting and placing them (ten per thread; the
+// 128-bit walk, done twice, cost more than the registers of its cache).
+template <class K> struct SuperRound {
+    static constexpr bool CACHE = true;
+    static constexpr int N = 10;  // k-mers per thread per round
+};
+
+// shared layout of k_scatter_super: staging for one round, then four S-entry arrays
 template <class K>
 struct SuperSmem {
-    K key[SC_THREADS * SC_ROUND];
-    uint16_t bits[SC_THREADS * SC_ROUND];
-    uint16_t sup[SC_THREADS * SC_ROUND];
+    K key[SC_THREADS * SuperRound<K>::N];
+    uint16_t bits[SC_THREADS * SuperRound<K>::N];
+    uint16_t sup[SC_THREADS * SuperRound<K>::N];
     uint32_t ws[33];
     uint32_t rounds, total;
     uint32_t hll[SC_HLL_REGS];  // this block's HyperLogLog registers (when the build asks for them)
@@ -1655,12 +1662,6 @@ struct SuperSmem {
     static size_t bytes(uint32_t S) { return sizeof(SuperSmem) + 4ull * S * sizeof(uint32_t); }
 };
 
-// 64-bit keys keep a round's k-mers in registers between counting and placing them; 128-bit
-// keys walk the round twice instead (their cache would cost too many registers)
-template <class K> struct SuperRound {
-    static constexpr bool CACHE = sizeof(K) == 8;
-    static constexpr int N = CACHE ? 10 : SC_ROUND;  // k-mers per thread per round
-};
 
 template <class K>
 __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_super(const uint8_t *text, unsigned long long n_text,

@@ -104,7 +104,6 @@ constexpr uint32_t AGG_SLOTS = 2048;         // shared-memory table of one fine 
 constexpr uint32_t AGG_TARGET = 896;         // distinct k-mers per fine bucket aimed for
 constexpr uint32_t CHUNK = 4096;             // occurrences per CTA in the fine passes
 constexpr int SC_THREADS = 256;              // super scatter: one read per thread
-constexpr int SC_ROUND = 16;                 // k-mers per thread per staging round
 constexpr int SC_HLL_REGS = 512;             // HyperLogLog registers kept by the super scatter
 // A super scatter without a counting pass first: every super bucket gets room for this share of
 // the mean bucket plus SC_SLACK; a bucket that needs more sets the overflow flag.
