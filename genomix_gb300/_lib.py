@@ -14,6 +14,8 @@ GX_EAGAIN = 14
 GX_ESTATE = 10
 GX_ECANCELLED = 11
 GX_EBUSY = 13
+GX_ETIMEOUT = 8
+CTX_TEST_WITHHOLD_COPIES = 1
 STATUS_NAMES = {
     0: "GX_OK", 1: "GX_EINVAL", 2: "GX_EINVAL_LINE", 3: "GX_EINVAL_NUMBER", 4: "GX_EREADID_RANGE",
     5: "GX_EREAD_TOO_SHORT", 6: "GX_ENOMEM", 7: "GX_ETABLE_FULL", 8: "GX_ETIMEOUT", 9: "GX_ECUDA",

@@ -147,6 +147,7 @@ gx_status gx_ctx_create(int device, const gx_ctx_opts *opts, gx_ctx **out) {
     c->mem_limit = (opts && opts->device_mem_limit) ? opts->device_mem_limit : (size_t)(0.9 * (double)fr);
     if (opts && opts->struct_size >= offsetof(gx_ctx_opts, test_alloc_fail_above) + sizeof(size_t))
         c->test_alloc_fail_above = opts->test_alloc_fail_above;
+    if (opts) c->test_flags = opts->flags;
     for (auto &e : c->marks) cudaEventCreate(&e);
     if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaStreamDestroy(c->stream);
@@ -537,20 +538,27 @@ static gx_status relayout_reference_parts(RunCtx &rc, uint32_t &nparts, unsigned
     const unsigned long long *bnd;
     uint64_t n_bnd;  // entries of bnd, the last one the total
     unsigned long long moved = 0;
+    uint32_t late = 0;  // a bulk copy of the regrouping that did not land in time
     if (one_pass) {
         const uint32_t tiles = by_bucket ? nparts : rl_tiles(N);
         const uint64_t ncnt = (uint64_t)P * tiles;
         unsigned long long *cnt;
+        uint32_t *d_late;
         void *scratch;
         if ((e = ar.alloc(cnt, ncnt + 1)) != GX_OK) return e;
         if ((e = ar.alloc(scratch, scan_scratch_bytes(ncnt, 8))) != GX_OK) return e;
+        if ((e = ar.alloc(d_late, 1)) != GX_OK) return e;
+        CK(cudaMemsetAsync(d_late, 0, 4, s));
+        const int withhold = (j->ctx->test_flags & GX_CTX_TEST_WITHHOLD_COPIES) ? 1 : 0;
         if (by_bucket)
             launch_rl_regroup_nodes((const uint8_t *)outp, nr->nkey, j->wide, j->k, nr->noff, nr->node_base, part_off,
-                                    d_part_nodes, nparts, P, cnt, scratch, (uint8_t *)nout, s);
+                                    d_part_nodes, nparts, P, cnt, scratch, (uint8_t *)nout, d_late, withhold, s);
         else
-            launch_rl_regroup_arrays((const uint8_t *)outp, rpart, rlen, roff, N, P, cnt, scratch, (uint8_t *)nout, s);
+            launch_rl_regroup_arrays((const uint8_t *)outp, rpart, rlen, roff, N, P, cnt, scratch, (uint8_t *)nout,
+                                     d_late, withhold, s);
         launch_rl_part_starts(cnt, tiles, P, total, bounds, s);
         CK(d2h_async(&moved, cnt + ncnt, 8, s));
+        CK(d2h_async(&late, d_late, 4, s));
         bnd = cnt;
         n_bnd = ncnt + 1;
     } else {
@@ -596,6 +604,11 @@ static gx_status relayout_reference_parts(RunCtx &rc, uint32_t &nparts, unsigned
     CK(d2h_async(hb.data(), bounds, (P + 1) * 8ull, s));
     CK(sync_stream(s));
     CK(cudaGetLastError());
+    if (late) {
+        cudaFreeAsync(groups, s);
+        fprintf(stderr, "gxgpu: the regrouping into the reference's parts timed out waiting for a bulk copy\n");
+        return GX_ETIMEOUT;
+    }
     if (moved != total || hb[0] != 0 || hb[P] != total) {
         cudaFreeAsync(groups, s);
         fprintf(stderr, "gxgpu: internal error: the regrouped records do not add up\n");

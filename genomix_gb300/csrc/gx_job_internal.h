@@ -47,6 +47,7 @@ struct gx_ctx {
     std::mutex mu;
     size_t mem_limit = 0;
     size_t test_alloc_fail_above = 0;  // testing: run allocations above this fail as out of memory
+    int test_flags = 0;                // testing: GX_CTX_TEST_* (gx_ctx_opts.flags)
     cudaEvent_t marks[16] = {};
     // the handle holds one reference and every job one more: a context destroyed while jobs
     // still live is freed with the last of them

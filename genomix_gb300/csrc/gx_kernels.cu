@@ -3330,10 +3330,16 @@ __device__ __forceinline__ void smem_copy_bytes(uint8_t *d, const uint8_t *s, ui
     for (; i < n; i++) d[i] = s[i];
 }
 
+constexpr long long RL_WAIT_CYCLES = 2000000000LL;  // about a second: a bulk copy takes microseconds
+
 // The tile's records in source order, 256 at a time.  A record lands after the earlier records
 // of its part (earlier rounds, earlier warps of this round, earlier lanes of its warp), so this
 // round's records of part d form one run of the output, starting where the part's previous run
-// ended.  The round's source bytes (one range) come in with 16-byte loads; each thread copies
+// ended.  The round's source bytes (one range, its ends rounded to 16 bytes) come in with one
+// bulk copy (TMA) issued by thread 0 and completed on an mbarrier, while the threads rank the
+// round's records; the waits are bounded: a copy that has not landed after about a second
+// (never expected; `withhold` makes it happen, for testing) sets *err, waits once more for the
+// copy and ends the CTA.  Each thread copies
 // its record into that run's image in shared memory, the image placed at the run's own 16-byte
 // alignment; each warp then writes whole runs out with aligned 16-byte stores (the ragged ends
 // byte by byte, one lane per byte).  A round whose range does not fit (a giant record) copies
@@ -3341,10 +3347,12 @@ __device__ __forceinline__ void smem_copy_bytes(uint8_t *d, const uint8_t *s, ui
 // the next tile's part offsets are loaded while the current round works.
 template <class Src>
 __global__ void __launch_bounds__(256) k_rl_move(const uint8_t *sbytes, Src src, uint32_t n_tiles, uint32_t nparts,
-                                                 const unsigned long long *off, uint8_t *dst) {
+                                                 const unsigned long long *off, uint8_t *dst, uint32_t *err,
+                                                 int withhold) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint8_t *stage = smem;                 // RL_STAGE + 16 (word reads may run 3 bytes past a record)
     uint8_t *img = smem + RL_STAGE + 16;   // RL_OUT
+    __shared__ unsigned long long bar;     // completion of the round's bulk copy
     __shared__ unsigned long long run[256];
     __shared__ unsigned long long wb[8][256];
     __shared__ unsigned long long sdst[256], ssrc[256];
@@ -3359,6 +3367,9 @@ __global__ void __launch_bounds__(256) k_rl_move(const uint8_t *sbytes, Src src,
     unsigned long long so = 0;
     if (tid < n) src.get(t, tid, n, d, len, so);
     run[tid] = tid < nparts ? off[(uint64_t)tid * n_tiles + t] : 0ull;
+    if (tid == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    uint32_t parity = 0;
     for (;;) {
         const bool live = j0 + tid < n;
         for (int w = 0; w < 8; w++) wb[w][tid] = 0;
@@ -3372,6 +3383,18 @@ __global__ void __launch_bounds__(256) k_rl_move(const uint8_t *sbytes, Src src,
             nj0 = 0;
             nn = nt < n_tiles ? src.tile_size(nt) : 0u;
         }
+        // the round's source range, brought in by one bulk copy while the records are ranked
+        // records this round; an empty bucket (no nodes) still takes one round, with nothing to move
+        const uint32_t cnt = n > j0 ? min(256u, n - j0) : 0u;
+        const unsigned long long lo = cnt ? ssrc[0] & ~15ull : 0ull;
+        const unsigned long long hi = cnt ? (ssrc[cnt - 1] + slen[cnt - 1] + 15) & ~15ull : 0ull;
+        const bool fits = hi - lo <= (unsigned long long)RL_STAGE;
+        const bool bulk = fits && hi > lo;
+        if (bulk && tid == 0 && !withhold) {
+            fence_proxy_async_smem();  // the last round's reads of the stage come first
+            mbar_arrive_expect_tx(&bar, (uint32_t)(hi - lo));
+            bulk_g2s(stage, sbytes + lo, (uint32_t)(hi - lo), &bar);
+        }
         uint32_t d2 = 256u + lane, len2 = 0;
         unsigned long long so2 = 0, run2 = 0;
         if (nt < n_tiles && nj0 + tid < nn) src.get(nt, nj0 + tid, nn, d2, len2, so2);
@@ -3381,17 +3404,14 @@ __global__ void __launch_bounds__(256) k_rl_move(const uint8_t *sbytes, Src src,
         uint32_t pre = 0;
         for (uint32_t m = same & ((1u << lane) - 1u); m; m &= m - 1) pre += slen[warp * 32 + __ffs(m) - 1];
         if (live && (same >> lane) == 1u) wb[warp][d] = (unsigned long long)pre + len;  // the group's last lane
-        // the round's source range; its loads go out first
-        // records this round; an empty bucket (no nodes) still takes one round, with nothing to move
-        const uint32_t cnt = n > j0 ? min(256u, n - j0) : 0u;
-        const unsigned long long lo = cnt ? ssrc[0] & ~15ull : 0ull;
-        const unsigned long long hi = cnt ? (ssrc[cnt - 1] + slen[cnt - 1] + 15) & ~15ull : 0ull;
-        const bool fits = hi - lo <= (unsigned long long)RL_STAGE;
-        if (fits) {
-            const uint32_t span = (uint32_t)(hi - lo);
-            const uint8_t *sb = sbytes + lo;
-            for (uint32_t x = 16u * tid; x < span; x += 16u * 256u)
-                *reinterpret_cast<uint4 *>(stage + x) = *reinterpret_cast<const uint4 *>(sb + x);
+        if (bulk) {
+            const bool late = !mbar_wait_bounded(&bar, parity, RL_WAIT_CYCLES);
+            if (__syncthreads_or(late)) {
+                if (tid == 0) atomicOr(err, 1u);
+                if (!withhold) mbar_wait_bounded(&bar, parity, 4 * RL_WAIT_CYCLES);  // the copy in flight
+                return;
+            }
+            parity ^= 1u;
         }
         __syncthreads();
         // this thread's part (tid): its run this round and the run's image slot
@@ -3604,36 +3624,36 @@ void launch_rl_index_nodes(const void *nkey, int wide, int k, const unsigned lon
 
 template <class Src>
 static void rl_regroup(const uint8_t *sbytes, Src src, uint32_t n_tiles, uint32_t nparts, unsigned long long *cnt,
-                       void *scratch, uint8_t *dst, cudaStream_t s) {
+                       void *scratch, uint8_t *dst, uint32_t *err, int withhold, cudaStream_t s) {
     const uint64_t ncnt = (uint64_t)nparts * n_tiles;
     const unsigned blocks = std::min<uint32_t>(n_tiles, 152u * 16u);
     t_launches += 2;
     k_rl_tile_bytes<Src><<<blocks, 256, 0, s>>>(src, n_tiles, nparts, cnt);
     exclusive_scan_u64(cnt, cnt, ncnt, cnt + ncnt, scratch, s);
     cudaFuncSetAttribute(k_rl_move<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize, RL_SMEM);
-    k_rl_move<Src><<<blocks, 256, RL_SMEM, s>>>(sbytes, src, n_tiles, nparts, cnt, dst);
+    k_rl_move<Src><<<blocks, 256, RL_SMEM, s>>>(sbytes, src, n_tiles, nparts, cnt, dst, err, withhold);
 }
 
 void launch_rl_regroup_arrays(const uint8_t *sbytes, const uint32_t *rpart, const uint32_t *rlen,
                               const unsigned long long *roff, uint64_t n, uint32_t nparts, unsigned long long *cnt,
-                              void *scratch, uint8_t *dst, cudaStream_t s) {
+                              void *scratch, uint8_t *dst, uint32_t *err, int withhold, cudaStream_t s) {
     if (!n) return;
     RecArrays src{rpart, rlen, roff, n};
-    rl_regroup(sbytes, src, rl_tiles(n), nparts, cnt, scratch, dst, s);
+    rl_regroup(sbytes, src, rl_tiles(n), nparts, cnt, scratch, dst, err, withhold, s);
 }
 
 void launch_rl_regroup_nodes(const uint8_t *sbytes, const void *nkey, int wide, int k, const uint32_t *noff,
                              const unsigned long long *node_base, const unsigned long long *part_off,
                              const uint32_t *part_nodes, uint32_t n_buckets, uint32_t nparts, unsigned long long *cnt,
-                             void *scratch, uint8_t *dst, cudaStream_t s) {
+                             void *scratch, uint8_t *dst, uint32_t *err, int withhold, cudaStream_t s) {
     if (!n_buckets) return;
     const int nb = (k + 3) / 4;
     if (wide) {
         RecNodes<u128> src{(const u128 *)nkey, noff, node_base, part_off, part_nodes, nb, nparts};
-        rl_regroup(sbytes, src, n_buckets, nparts, cnt, scratch, dst, s);
+        rl_regroup(sbytes, src, n_buckets, nparts, cnt, scratch, dst, err, withhold, s);
     } else {
         RecNodes<uint64_t> src{(const uint64_t *)nkey, noff, node_base, part_off, part_nodes, nb, nparts};
-        rl_regroup(sbytes, src, n_buckets, nparts, cnt, scratch, dst, s);
+        rl_regroup(sbytes, src, n_buckets, nparts, cnt, scratch, dst, err, withhold, s);
     }
 }
 

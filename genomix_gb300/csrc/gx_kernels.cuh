@@ -217,13 +217,15 @@ void launch_rl_index_nodes(const void *nkey, int wide, int k, const unsigned lon
 // Up to 256 parts: per tile and part byte counts into cnt ([part][tile], parts x tiles + 1 entries,
 // scanned in place, the total last), then the records moved to their places in dst.  Tiles are
 // RL_TILE records of the arrays, or the buckets of the partitioned build.
+// The source bytes of each round arrive by bulk copy; *err is set when a copy did not land
+// within about a second (withhold != 0: the copies are not issued, for testing that path).
 void launch_rl_regroup_arrays(const uint8_t *sbytes, const uint32_t *rpart, const uint32_t *rlen,
                               const unsigned long long *roff, uint64_t n, uint32_t nparts, unsigned long long *cnt,
-                              void *scratch, uint8_t *dst, cudaStream_t s);
+                              void *scratch, uint8_t *dst, uint32_t *err, int withhold, cudaStream_t s);
 void launch_rl_regroup_nodes(const uint8_t *sbytes, const void *nkey, int wide, int k, const uint32_t *noff,
                              const unsigned long long *node_base, const unsigned long long *part_off,
                              const uint32_t *part_nodes, uint32_t n_buckets, uint32_t nparts, unsigned long long *cnt,
-                             void *scratch, uint8_t *dst, cudaStream_t s);
+                             void *scratch, uint8_t *dst, uint32_t *err, int withhold, cudaStream_t s);
 void launch_rl_part_starts(const unsigned long long *off, uint32_t n_tiles, uint32_t nparts, unsigned long long total,
                            unsigned long long *bounds, cudaStream_t s);
 void launch_rl_bounds(const uint32_t *rpart, const uint32_t *perm, uint64_t n, uint32_t nparts,

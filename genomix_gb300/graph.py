@@ -89,10 +89,10 @@ class PinnedBuffer:
 class Context:
     """A device and its stream (replaces the Hyracks cluster-controller connection)."""
 
-    def __init__(self, device=0, mem_limit=0, test_alloc_fail_above=0):
+    def __init__(self, device=0, mem_limit=0, test_alloc_fail_above=0, test_flags=0):
         L = _lib.load()
         self._L = L
-        opts = _lib.CtxOpts(ctypes.sizeof(_lib.CtxOpts), mem_limit, 0, int(test_alloc_fail_above))
+        opts = _lib.CtxOpts(ctypes.sizeof(_lib.CtxOpts), mem_limit, int(test_flags), int(test_alloc_fail_above))
         h = ctypes.c_void_p()
         _check(L.gx_ctx_create(device, ctypes.byref(opts), ctypes.byref(h)), "gx_ctx_create")
         self.h = h.value

@@ -51,7 +51,7 @@ typedef enum gx_status {
                                  ReadsKeyValueParserFactory.java:152-155 */
     GX_ENOMEM = 6,            /* device or pinned allocation failed */
     GX_ETABLE_FULL = 7,       /* a hash-table partition overflowed its probe limit */
-    GX_ETIMEOUT = 8,          /* a bounded device wait ran out */
+    GX_ETIMEOUT = 8,          /* a bounded device wait ran out (a bulk copy that did not land) */
     GX_ECUDA = 9,             /* a CUDA runtime call failed */
     GX_ESTATE = 10,           /* call out of order (e.g. emit before run) */
     GX_ECANCELLED = 11,       /* job cancelled (serving) */
@@ -73,10 +73,15 @@ enum {
 typedef struct gx_ctx gx_ctx;
 typedef struct gx_job gx_job;
 
+/* gx_ctx_opts.flags (testing only): the bulk copies of the regrouping into the reference's
+   parts are not issued, so its bounded waits run out (after about a second) and the job
+   returns GX_ETIMEOUT; lets tests reach the timeout path without a fault. */
+#define GX_CTX_TEST_WITHHOLD_COPIES 1
+
 typedef struct gx_ctx_opts {
     size_t struct_size;       /* sizeof(gx_ctx_opts) */
     size_t device_mem_limit;  /* bytes the context may hold on the device; 0 = 90% of free */
-    int flags;                /* reserved, 0 */
+    int flags;                /* 0, or GX_CTX_TEST_* flags (testing only) */
     size_t test_alloc_fail_above; /* testing only: any working-buffer allocation of a run on this
                                      context larger than this many bytes fails as if the device
                                      were out of memory (0 = off); lets tests reach the

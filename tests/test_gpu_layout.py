@@ -163,3 +163,29 @@ def test_driver_part_files_match_reference_parts(ctx, tmp_path):
         mine = gx.seqfile_read((tmp_path / "out" / f"part-{q}").read_bytes())
         theirs = ref.records[ref.part_offsets[q]:ref.part_offsets[q + 1]]
         assert go.normalize(mine) == go.normalize(theirs), q
+
+
+def test_bulk_copy_wait_times_out_cleanly():
+    """The regrouping's source bytes arrive by bulk copy with a bounded wait.  A context with the
+    testing flag that withholds those copies makes every wait run out: the job returns
+    GX_ETIMEOUT after about a second, and the device stays usable (a normal context then builds
+    the same input in the same layout, equal to the oracle's parts)."""
+    from genomix_gb300 import _lib
+    text = synth.plain_cpu(max_reads=3000).text
+    with gx.Context(0, test_flags=_lib.CTX_TEST_WITHHOLD_COPIES) as bad:
+        job = gx.GraphBuildJob(bad, 21, out_parts=8, layout="reference")
+        job.add_input(text)
+        with pytest.raises(gx.GraphBuildError) as ei:
+            job.run()
+        assert ei.value.status == _lib.GX_ETIMEOUT
+        job.close()
+    with gx.Context(0) as good:
+        job = gx.GraphBuildJob(good, 21, out_parts=8, layout="reference")
+        job.add_input(text)
+        job.run()
+        ref = go.build_graph(text, 21, threads=4, parts=8)
+        for q in range(8):
+            got = job.records(part=q)
+            want = ref.records[ref.part_offsets[q]:ref.part_offsets[q + 1]]
+            assert go.normalize(got) == go.normalize(want), q
+        job.close()
