@@ -2023,67 +2023,59 @@ void launch_heads_part(int wide, const uint8_t *text, uint64_t n_text, const Lin
 }
 
 // ---- C --------------------------------------------------------------------------------------
-// The shared table of one bucket.  64-bit keys keep a slot's key, count and flags side by side,
-// so one 16-byte load reads all three; 128-bit keys keep them in three arrays.  Stored key =
-// value + 1, 0 = empty; every claim is a compare-and-swap, so a racing claim is never missed.
-template <class K> struct AggTab;
-template <> struct AggTab<uint64_t> {
-    struct Slot {
-        unsigned long long key1;
-        uint32_t cnt, meta;
-    };
-    Slot s[AGG_SLOTS];
-    __device__ __forceinline__ unsigned long long *keyp(uint32_t i) { return &s[i].key1; }
-    __device__ __forceinline__ uint32_t *cntp(uint32_t i) { return &s[i].cnt; }
-    __device__ __forceinline__ uint32_t *metap(uint32_t i) { return &s[i].meta; }
-    __device__ __forceinline__ uint64_t key1(uint32_t i) const { return s[i].key1; }
-    // the key and the flags of slot i in one load
-    __device__ __forceinline__ uint64_t key1_meta(uint32_t i, uint32_t &meta) const {
-        const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(&s[i]);
-        meta = (uint32_t)(v.y >> 32);
-        return v.x;
-    }
-    __device__ __forceinline__ int insert(uint64_t key, uint32_t h, uint32_t &claimed) {
+template <class K> struct AggTable;
+template <> struct AggTable<uint64_t> {
+    // stored key = V + 1, 0 = empty; every probe is a CAS so a racing claim is never missed
+    __device__ __forceinline__ static int insert(uint64_t *key1, uint64_t key, uint32_t h, uint32_t &claimed) {
         const unsigned long long want = (unsigned long long)key + 1ULL;
         uint32_t i = h & (AGG_SLOTS - 1);
         for (uint32_t n = 0; n < AGG_SLOTS; n++) {
-            unsigned long long cur = *((volatile unsigned long long *)keyp(i));
-            if (cur != want) cur = atomicCAS(keyp(i), 0ULL, want);
+            unsigned long long cur = ((volatile unsigned long long *)key1)[i];
+            if (cur != want) cur = atomicCAS((unsigned long long *)&key1[i], 0ULL, want);
             if (cur == 0ULL) claimed = 1;
             if (cur == 0ULL || cur == want) return (int)i;
             i = (i + 1) & (AGG_SLOTS - 1);
         }
         return -1;
     }
-};
-template <> struct AggTab<u128> {
-    u128 k1[AGG_SLOTS];
-    uint32_t cnt[AGG_SLOTS];
-    uint32_t meta[AGG_SLOTS];
-    __device__ __forceinline__ u128 *keyp(uint32_t i) { return &k1[i]; }
-    __device__ __forceinline__ uint32_t *cntp(uint32_t i) { return &cnt[i]; }
-    __device__ __forceinline__ uint32_t *metap(uint32_t i) { return &meta[i]; }
-    __device__ __forceinline__ u128 key1(uint32_t i) const { return k1[i]; }
-    __device__ __forceinline__ u128 key1_meta(uint32_t i, uint32_t &m) const {
-        m = 0;  // not read here: the flags are OR-ed in every time
-        return k1[i];
+    __device__ __forceinline__ static int find(const uint64_t *key1, uint64_t key, uint32_t h) {
+        const uint64_t want = key + 1;
+        uint32_t i = h & (AGG_SLOTS - 1);
+        for (uint32_t n = 0; n < AGG_SLOTS; n++) {
+            const uint64_t cur = key1[i];
+            if (cur == want) return (int)i;
+            if (cur == 0) return -1;
+            i = (i + 1) & (AGG_SLOTS - 1);
+        }
+        return -1;
     }
-    __device__ __forceinline__ int insert(u128 key, uint32_t h, uint32_t &claimed) {
+};
+template <> struct AggTable<u128> {
+    __device__ __forceinline__ static int insert(u128 *key1, u128 key, uint32_t h, uint32_t &claimed) {
         const u128 want = key + 1;
         const unsigned long long wlo = (unsigned long long)want, whi = (unsigned long long)(want >> 64);
         uint32_t i = h & (AGG_SLOTS - 1);
         for (uint32_t n = 0; n < AGG_SLOTS; n++) {
             unsigned long long clo, chi;
-            cas128_shared(&k1[i], 0ULL, 0ULL, wlo, whi, clo, chi);
+            cas128_shared(&key1[i], 0ULL, 0ULL, wlo, whi, clo, chi);
             if (clo == 0ULL && chi == 0ULL) claimed = 1;
             if ((clo == 0ULL && chi == 0ULL) || (clo == wlo && chi == whi)) return (int)i;
             i = (i + 1) & (AGG_SLOTS - 1);
         }
         return -1;
     }
+    __device__ __forceinline__ static int find(const u128 *key1, u128 key, uint32_t h) {
+        const u128 want = key + 1;
+        uint32_t i = h & (AGG_SLOTS - 1);
+        for (uint32_t n = 0; n < AGG_SLOTS; n++) {
+            const u128 cur = key1[i];
+            if (cur == want) return (int)i;
+            if (cur == 0) return -1;
+            i = (i + 1) & (AGG_SLOTS - 1);
+        }
+        return -1;
+    }
 };
-static_assert(sizeof(AggTab<uint64_t>) == AGG_SLOTS * 16 && sizeof(AggTab<u128>) == AGG_SLOTS * 24,
-              "the table is cleared in 16-byte stores");
 
 // Home slot of a key in a bucket's shared table: the top 11 bits of a multiplicative hash (the
 // bucket itself was picked by other bits of the MurmurHash3 finaliser).
@@ -2104,8 +2096,7 @@ static_assert(AGG_SLOTS == 1u << 11, "agg_home gives 11-bit slots");
 // cluster (a cluster that wraps past the last slot is numbered last).  Five phases with a
 // barrier between them:
 //   1. read heads (which claim or find their k-mer's slot and mark the set they belong to)
-//      and occurrences inserted: count += 1, edge bits OR-ed in unless the home-slot read (key,
-//      count and flags in one load, 64-bit keys) already showed them;
+//      and occurrences inserted: count += 1, edge bits OR-ed in;
 //   2. occupancy bitmap (warp ballots) and per-warp counts;
 //   3. every node's rank: its cluster's start, the occupied slots before it, its place by key
 //      in the cluster; key, count/meta word and base record size out;
@@ -2117,7 +2108,9 @@ static_assert(AGG_SLOTS == 1u << 11, "agg_home gives 11-bit slots");
 // scans sizes that include them (the general path, rare).
 template <class K>
 struct AggSmem {
-    AggTab<K> tab;                     // keys, occurrence counts, flags (edge bits, read-head sets)
+    K key1[AGG_SLOTS];                 // key + 1; 0 = empty
+    uint32_t cnt[AGG_SLOTS];           // occurrences
+    uint32_t meta[AGG_SLOTS];          // edge bits, read-head set flags
     uint32_t nbytes[AGG_SLOTS];        // record bytes per node in rank order, then offsets
     uint16_t ord[AGG_SLOTS];           // slot of the node of each rank
     uint16_t rank_of_slot[AGG_SLOTS];
@@ -2234,8 +2227,12 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
     }
     {
         const uint4 z = make_uint4(0, 0, 0, 0);
-        uint4 *t4 = reinterpret_cast<uint4 *>(&sm.tab);
-        for (uint32_t i = threadIdx.x; i < sizeof(AggTab<K>) / 16; i += blockDim.x) t4[i] = z;
+        uint4 *k4 = reinterpret_cast<uint4 *>(sm.key1);
+        for (uint32_t i = threadIdx.x; i < AGG_SLOTS * sizeof(K) / 16; i += blockDim.x) k4[i] = z;
+        for (uint32_t i = threadIdx.x; i < AGG_SLOTS / 4; i += blockDim.x) {
+            reinterpret_cast<uint4 *>(sm.cnt)[i] = z;
+            reinterpret_cast<uint4 *>(sm.meta)[i] = z;
+        }
     }
     if (threadIdx.x == 0) {
         sm.n = 0;
@@ -2249,12 +2246,12 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         if (threadIdx.x < hc) {
             const K key = (K)(((u128)p_h.khi << 64) | p_h.klo);
             uint32_t claimed = 0;
-            const int sl = sm.tab.insert(key, agg_home(key), claimed);
+            const int sl = AggTable<K>::insert(sm.key1, key, agg_home(key), claimed);
             if (sl < 0) {
                 sm.fail = 1;
             } else {
                 if (claimed) atomicAdd(&sm.n, 1u);
-                atomicOr(sm.tab.metap(sl), (p_h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
+                atomicOr(&sm.meta[sl], (p_h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
                 p_slot = (uint32_t)sl;
             }
         }
@@ -2264,13 +2261,13 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             const Head h = a.heads[r];
             const K key = (K)(((u128)h.khi << 64) | h.klo);
             uint32_t claimed = 0;
-            const int sl = sm.tab.insert(key, agg_home(key), claimed);
+            const int sl = AggTable<K>::insert(sm.key1, key, agg_home(key), claimed);
             if (sl < 0) {
                 sm.fail = 1;
                 continue;
             }
             if (claimed) atomicAdd(&sm.n, 1u);
-            atomicOr(sm.tab.metap(sl), (h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
+            atomicOr(&sm.meta[sl], (h.uuid >> 40) != 0 ? META_FLIPPED : META_UNFLIPPED);
             a.heads[r].slot = (uint32_t)sl;
         }
     }
@@ -2288,12 +2285,12 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         // occurrence whose key is not in its home slot takes the probe with compare-and-swap.
 #pragma unroll
         for (int g = 0; g < BATCH; g += 4) {
-            uint32_t hm[4], seen[4];
+            uint32_t hm[4];
             K cur[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 hm[u] = agg_home(kk[g + u]);
-                cur[u] = sm.tab.key1_meta(hm[u], seen[u]);
+                cur[u] = sm.key1[hm[u]];
             }
 #pragma unroll
             for (int u = 0; u < 4; u++) {
@@ -2301,19 +2298,17 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
                 const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
                 if (i >= M) continue;
                 int sl = (int)hm[u];
-                uint32_t have = seen[u];  // flags already set (bits are never cleared)
                 if (cur[u] != kk[q] + 1) {
                     uint32_t claimed = 0;
-                    sl = sm.tab.insert(kk[q], hm[u], claimed);
+                    sl = AggTable<K>::insert(sm.key1, kk[q], hm[u], claimed);
                     if (sl < 0) {
                         sm.fail = 1;
                         continue;
                     }
                     if (claimed) atomicAdd(&sm.n, 1u);
-                    have = 0;
                 }
-                atomicAdd(sm.tab.cntp(sl), 1u);  // no result used: both are fire-and-forget reductions
-                if (bb[q] & ~have) atomicOr(sm.tab.metap(sl), bb[q]);
+                atomicAdd(&sm.cnt[sl], 1u);  // no result used: both are fire-and-forget reductions
+                if (bb[q]) atomicOr(&sm.meta[sl], bb[q]);
             }
         }
     }
@@ -2327,7 +2322,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
     uint32_t myocc = 0;
 #pragma unroll
     for (int q = 0; q < 8; q++) {
-        const uint32_t b = __ballot_sync(full, sm.tab.key1(warp * 256 + q * 32 + lane) != (K)0);
+        const uint32_t b = __ballot_sync(full, sm.key1[warp * 256 + q * 32 + lane] != (K)0);
         if (lane == q) myocc = b;
     }
     const uint32_t pc = lane < 8 ? __popc(myocc) : 0u;
@@ -2375,7 +2370,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         }
         const uint32_t slot = warp * 256 + q * 32 + bit;
         const uint32_t before = wbase + idx;  // occupied slots before this one
-        const K mine = sm.tab.key1(slot);
+        const K mine = sm.key1[slot];
         const uint32_t sl_prev = (slot - 1) & (AGG_SLOTS - 1), sl_next = (slot + 1) & (AGG_SLOTS - 1);
         uint32_t pre_c0, within = 0;
         if (!((sm.occ[sl_prev >> 5] >> (sl_prev & 31)) & 1u) && !((sm.occ[sl_next >> 5] >> (sl_next & 31)) & 1u)) {
@@ -2387,7 +2382,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             pre_c0 = c0 <= slot ? before - (slot - c0) : n - (AGG_SLOTS - c0);
             for (uint32_t j = c0;; j = (j + 1) & (AGG_SLOTS - 1)) {
                 if (!((sm.occ[j >> 5] >> (j & 31)) & 1u)) break;
-                within += sm.tab.key1(j) < mine ? 1u : 0u;
+                within += sm.key1[j] < mine ? 1u : 0u;
             }
         }
         const uint32_t rank = pre_c0 - z + within;
@@ -2397,7 +2392,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         }
         sm.rank_of_slot[slot] = (uint16_t)rank;
         sm.ord[rank] = (uint16_t)slot;
-        const uint32_t cnt = *sm.tab.cntp(slot), meta = *sm.tab.metap(slot);
+        const uint32_t cnt = sm.cnt[slot], meta = sm.meta[slot];
         nkey[rank] = mine - 1;
         ncm[rank] = (unsigned long long)cnt | ((unsigned long long)meta << 32);
         if (cnt >= (1u << 24)) inexact++;
@@ -2486,7 +2481,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             if (wkeep) {
                 const int first = __ffs(node_mask) - 1;
                 const uint32_t cu = __popc(node_mask & ~flip_mask), cf = __popc(node_mask & flip_mask);
-                const uint32_t meta = *sm.tab.metap(w_slot);
+                const uint32_t meta = sm.meta[w_slot];
                 const uint32_t st = __popc(wkeep_mask & ((1u << first) - 1u));  // kept index of the node's first
                 HeadOut ho;
                 ho.uuid = w_uuid;
@@ -2625,7 +2620,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         const uint32_t cu = fl - st, cf = kept_lower_bound(hk, kept, rbase + (1ULL << 37)) - fl;
         const unsigned long long pre = key & ((1ULL << 36) - 1);
         const unsigned long long pre0 = hk[st] & ((1ULL << 36) - 1);
-        const uint32_t meta = *sm.tab.metap(sm.ord[rank]);
+        const uint32_t meta = sm.meta[sm.ord[rank]];
         const uint32_t pos = sm.nbytes[rank] + 8 + keylen + 1 + edge_bytes(meta, nb) + 5 +
                              ((flipped && cu > 0) ? 5 : 0) + (uint32_t)(pre - pre0);
         const uint32_t r = hv[i];
