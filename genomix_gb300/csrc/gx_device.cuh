@@ -104,25 +104,6 @@ template <> struct KeyOps<u128> {
     __device__ __forceinline__ static uint32_t byte_at(u128 v, int i) { return (uint32_t)(v >> (8 * i)) & 0xffu; }
 };
 
-// The same neighbour from X and its reverse complement RX (computed once per node): the
-// reverse complement of a shifted k-mer is the other way's shift of RX with the complement of
-// the new base, so no edge needs a reverse complement of its own.
-//   FR: rc((X >> 2) | e << 2(k-1)) = ((RX << 2) | (3 - e)) & mask
-//   RF: rc(((X << 2) | e) & mask) = (RX >> 2) | (3 - e) << 2(k-1)
-template <class K>
-__device__ __forceinline__ K edge_neighbor_rc(K x, K rx, int t, int e, int k) {
-    switch (t) {
-        case 0:  // FF
-            return (x >> 2) | ((K)e << (2 * (k - 1)));
-        case 1:  // FR
-            return ((rx << 2) | (K)(3 - e)) & KeyOps<K>::mask(k);
-        case 2:  // RF
-            return (rx >> 2) | ((K)(3 - e) << (2 * (k - 1)));
-        default:  // RR
-            return ((x << 2) | (K)e) & KeyOps<K>::mask(k);
-    }
-}
-
 // Neighbour Y of node X for edge bit (t, e), see the file header.
 template <class K>
 __device__ __forceinline__ K edge_neighbor(K x, int t, int e, int k) {

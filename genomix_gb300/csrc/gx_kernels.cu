@@ -2985,7 +2985,6 @@ __global__ void __launch_bounds__(WRITER_WARPS * 32, sizeof(K) == 8 ? 4 : 3) k_e
                 // the edge lists in FF, FR, RF, RR order; a list's neighbours in the order of
                 // their extension base (the reference's lists are unordered sets)
                 uint32_t lists = active & 15u;
-                const K rkey = (lists & 6u) ? KeyOps<K>::revcomp(key, k) : (K)0;  // for FR and RF
                 while (lists) {
                     const int t = __ffs(lists) - 1;
                     lists &= lists - 1;
@@ -2995,7 +2994,7 @@ __global__ void __launch_bounds__(WRITER_WARPS * 32, sizeof(K) == 8 ? 4 : 3) k_e
                         const int e = __ffs(m) - 1;
                         m &= m - 1;
                         o.be32((uint32_t)k);
-                        put_key<K>(o, edge_neighbor_rc<K>(key, rkey, t, e, k), nb);
+                        put_key<K>(o, edge_neighbor<K>(key, t, e, k), nb);
                     }
                 }
                 if (!heads) {
