@@ -140,7 +140,7 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
 
     // ---- parse the whole batch, then find each sample's lines and reads ----
     const uint64_t tiles = line_tiles(n_text);
-    uint32_t *tile_cnt, *d_nlines, *d_scnt, *d_hll, *line_base, *read_base;
+    uint32_t *tile_cnt, *d_nlines, *line_base, *read_base;
     unsigned long long *d_tb;
     void *scratch;
     const size_t scratch_bytes = std::max(scan_scratch_bytes(std::max<uint64_t>(tiles, 1), 8),
@@ -148,13 +148,12 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
     if ((e = ar.alloc(tile_cnt, tiles + 1)) != GX_OK) return e;
     if ((e = ar.alloc(d_nlines, 4)) != GX_OK) return e;
     if ((e = ar.alloc(scratch, scratch_bytes)) != GX_OK) return e;
-    if ((e = ar.alloc(d_scnt, (size_t)n * MAX_SUPERS)) != GX_OK) return e;
-    if ((e = ar.alloc(d_hll, (size_t)n * HLL_REGS)) != GX_OK) return e;
+    unsigned long long *d_occ;
+    if ((e = ar.alloc(d_occ, n)) != GX_OK) return e;
     if ((e = ar.alloc(line_base, n + 1)) != GX_OK) return e;
     if ((e = ar.alloc(read_base, n + 1)) != GX_OK) return e;
     if ((e = ar.alloc(d_tb, n + 1)) != GX_OK) return e;
-    CK(cudaMemsetAsync(d_scnt, 0, (size_t)n * MAX_SUPERS * 4, s));
-    CK(cudaMemsetAsync(d_hll, 0, (size_t)n * HLL_REGS * 4, s));
+    CK(cudaMemsetAsync(d_occ, 0, (size_t)n * 8, s));
     CK(cudaMemcpyAsync(d_tb, tb.data(), (n + 1) * 8ull, cudaMemcpyHostToDevice, s));
     launch_count_lines(text, n_text, tile_cnt, s);
     exclusive_scan_u32(tile_cnt, tile_cnt, tiles, d_nlines, scratch, s);
@@ -175,25 +174,25 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
     exclusive_scan_u32(nvalid, nvalid, n_lines, d_nlines + 1, scratch, s);
     launch_read_list(lflags, nvalid, lines, n_lines, k, reads, d_st, s);
     launch_sample_bounds(d_tb, n, line_end, n_lines, nvalid, d_nlines + 1, line_base, read_base, s);
-    launch_count_occ_batch(wide, text, n_text, lines, reads, read_base, n, 2 * n_lines, k, d_scnt, d_hll, s);
+    launch_sample_occ(lines, reads, 2 * n_lines, k, SampleMap{read_base, nullptr, n}, d_occ, s);
     CK(cudaEventRecord(tm.ev[1], s));
     DevStatus hs;
-    std::vector<uint32_t> h_lb(n + 1), h_rb(n + 1), h_scnt((size_t)n * MAX_SUPERS), h_hll((size_t)n * HLL_REGS);
+    std::vector<uint32_t> h_lb(n + 1), h_rb(n + 1);
+    std::vector<unsigned long long> occ(n, 0);
     CK(d2h_async(&hs, d_st, sizeof hs, s));
     CK(d2h_async(h_lb.data(), line_base, (n + 1) * 4ull, s));
     CK(d2h_async(h_rb.data(), read_base, (n + 1) * 4ull, s));
-    CK(d2h_async(h_scnt.data(), d_scnt, h_scnt.size() * 4, s));
-    CK(d2h_async(h_hll.data(), d_hll, h_hll.size() * 4, s));
+    CK(d2h_async(occ.data(), d_occ, (size_t)n * 8, s));
     CK(sync_stream(s));
     CK(cudaGetLastError());
     if (hs.parse_err != ~0ULL) return BATCH_FALLBACK;  // every job reruns alone for its own status
 
     const uint32_t n_reads = h_rb[n];
+    // before any count: the occurrences bound each sample's distinct k-mers (they set its super
+    // buckets); the super scatter's HyperLogLog registers then set its fine buckets
     std::vector<double> d_est(n);
-    std::vector<unsigned long long> occ(n, 0);
     for (uint32_t i = 0; i < n; i++) {
-        for (uint32_t q = 0; q < MAX_SUPERS; q++) occ[i] += h_scnt[(size_t)i * MAX_SUPERS + q];
-        d_est[i] = h_rb[i + 1] > h_rb[i] ? hll_estimate(&h_hll[(size_t)i * HLL_REGS]) : 0.0;
+        d_est[i] = (double)occ[i];
         gx_stats &st = jobs[i]->st;
         st.lines = h_lb[i + 1] - h_lb[i];
         st.reads = h_rb[i + 1] - h_rb[i];
@@ -210,32 +209,39 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
 
     double safety = 1.15;
     const double target = bucket_target(jobs[0]->eff_load_factor);  // one fill for the pass
+    const uint32_t tpr = (uint32_t)jobs[0]->eff_threads_per_read;
+    // The first pass scatters without a counting pass, as a single job does: every super bucket
+    // gets room for 1.3 x its sample's mean plus SC_SLACK, and the scatter gathers each sample's
+    // HyperLogLog registers, which then size its fine buckets.  A bucket that runs out of room
+    // (a k-mer repeated very many times) makes the batch count its samples exactly and go on with
+    // exact offsets.
+    bool counted = false;
+    std::vector<uint32_t> h_scnt, h_hll;  // the counting pass's, when it ran
     for (int attempt = 0;; attempt++) {
         std::vector<SamplePlan> plans;
         uint32_t S = 0, P = 0;
         if (!plan_batch(d_est, safety, target, plans, S, P)) return BATCH_FALLBACK;
-        // super counts at each sample's resolution, offsets and CHUNK-sized pieces
+        // super offsets: exact counts, or room per bucket
         std::vector<unsigned long long> soff(S + 1, 0);
+        std::vector<uint32_t> scount(S, 0);
         std::vector<SuperInfo> sinfo(S);
         for (uint32_t i = 0; i < n; i++) {
             const SamplePlan &pl = plans[i];
             const uint32_t Si = 1u << pl.log_s, fold = MAX_SUPERS >> pl.log_s;
+            const unsigned long long room =
+                std::min<unsigned long long>(0xfffffff0ULL, (unsigned long long)((double)occ[i] / Si * SC_ROOM) + SC_SLACK);
             for (uint32_t q = 0; q < Si; q++) {
-                unsigned long long cnt = 0;
-                for (uint32_t t = 0; t < fold; t++) cnt += h_scnt[(size_t)i * MAX_SUPERS + q * fold + t];
+                unsigned long long cnt = room;
+                if (counted) {
+                    cnt = 0;
+                    for (uint32_t t = 0; t < fold; t++) cnt += h_scnt[(size_t)i * MAX_SUPERS + q * fold + t];
+                    scount[pl.super_base + q] = (uint32_t)cnt;
+                }
                 soff[pl.super_base + q + 1] = cnt;
-                sinfo[pl.super_base + q] = SuperInfo{pl.fine_base + q * pl.F, pl.F, pl.log_s, 0};
             }
         }
         for (uint32_t g = 0; g < S; g++) soff[g + 1] += soff[g];
-        std::vector<ulonglong2> chunks;
-        chunks.reserve(n_occ / CHUNK + S + 1);
-        for (uint32_t g = 0; g < S; g++)
-            for (unsigned long long st = soff[g]; st < soff[g + 1]; st += CHUNK) {
-                const unsigned long long len = std::min<unsigned long long>(CHUNK, soff[g + 1] - st);
-                chunks.push_back(make_ulonglong2(st, ((unsigned long long)g << 32) | len));
-            }
-        const uint32_t n_chunks = (uint32_t)chunks.size();
+        const unsigned long long occ_room = counted ? n_occ : soff[S];
 
         RunArena tar(s);
         uint8_t *okey_b, *okey2_b;
@@ -248,13 +254,90 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         SamplePlan *d_plan;
         SuperInfo *d_sinfo;
         void *pscratch;
-        if ((e = tar.alloc(okey_b, n_occ * kb)) != GX_OK) return e;
-        if ((e = tar.alloc(okey2_b, n_occ * kb)) != GX_OK) return e;
-        if ((e = tar.alloc(obits, n_occ)) != GX_OK) return e;
-        if ((e = tar.alloc(obits2, n_occ)) != GX_OK) return e;
+        if ((e = tar.alloc(okey_b, occ_room * kb)) != GX_OK) return e;
+        if ((e = tar.alloc(obits, occ_room)) != GX_OK) return e;
         if ((e = tar.alloc(d_soff, S + 1)) != GX_OK) return e;
-        if ((e = tar.alloc(d_chunks, std::max<uint32_t>(n_chunks, 1))) != GX_OK) return e;
         if ((e = tar.alloc(s_cur, S)) != GX_OK) return e;
+        if ((e = tar.alloc(d_plan, n)) != GX_OK) return e;
+        void *okey = okey_b;
+        CK(cudaMemcpyAsync(d_soff, soff.data(), (S + 1) * 8ull, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(s_cur, 0, S * 4ull, s));
+        const SampleMap smap{read_base, d_plan, n};
+        CK(cudaEventRecord(tm.ev[2], s));
+        if (!counted) {
+            uint32_t *d_shll, *d_ovf;
+            if ((e = tar.alloc(d_shll, (size_t)n * SC_HLL_REGS)) != GX_OK) return e;
+            if ((e = tar.alloc(d_ovf, 1)) != GX_OK) return e;
+            CK(cudaMemsetAsync(d_shll, 0, (size_t)n * SC_HLL_REGS * 4, s));
+            CK(cudaMemsetAsync(d_ovf, 0, 4, s));
+            CK(cudaMemcpyAsync(d_plan, plans.data(), n * sizeof(SamplePlan), cudaMemcpyHostToDevice, s));
+            launch_scatter_super(wide, text, n_text, lines, reads, n_reads, k, smap, S, d_soff, s_cur, okey, obits,
+                                 0u, d_shll, d_ovf, s, tpr);
+            std::vector<uint32_t> hh((size_t)n * SC_HLL_REGS);
+            uint32_t ovf = 0;
+            CK(d2h_async(scount.data(), s_cur, S * 4ull, s));
+            CK(d2h_async(hh.data(), d_shll, hh.size() * 4, s));
+            CK(d2h_async(&ovf, d_ovf, 4, s));
+            CK(sync_stream(s));
+            CK(cudaGetLastError());
+            if (ovf) {
+                // count every sample exactly, then scatter again into exact offsets (not an attempt)
+                tar.release();
+                uint32_t *d_scnt, *d_hll;
+                if ((e = ar.alloc(d_scnt, (size_t)n * MAX_SUPERS)) != GX_OK) return e;
+                if ((e = ar.alloc(d_hll, (size_t)n * HLL_REGS)) != GX_OK) return e;
+                CK(cudaMemsetAsync(d_scnt, 0, (size_t)n * MAX_SUPERS * 4, s));
+                CK(cudaMemsetAsync(d_hll, 0, (size_t)n * HLL_REGS * 4, s));
+                launch_count_occ_batch(wide, text, n_text, lines, reads, read_base, n, n_reads, k, d_scnt, d_hll, s);
+                h_scnt.resize((size_t)n * MAX_SUPERS);
+                h_hll.resize((size_t)n * HLL_REGS);
+                CK(d2h_async(h_scnt.data(), d_scnt, h_scnt.size() * 4, s));
+                CK(d2h_async(h_hll.data(), d_hll, h_hll.size() * 4, s));
+                CK(sync_stream(s));
+                CK(cudaGetLastError());
+                for (uint32_t i = 0; i < n; i++)
+                    d_est[i] = h_rb[i + 1] > h_rb[i] ? hll_estimate(&h_hll[(size_t)i * HLL_REGS]) : 0.0;
+                counted = true;
+                attempt--;
+                continue;
+            }
+            // each sample's fine buckets from its HyperLogLog estimate (its super buckets stay)
+            uint64_t fb = 0;
+            for (uint32_t i = 0; i < n; i++) {
+                SamplePlan &pl = plans[i];
+                const double dist = h_rb[i + 1] > h_rb[i] ? hll_estimate(&hh[(size_t)i * SC_HLL_REGS], SC_HLL_REGS) : 0.0;
+                const uint64_t Pi = (uint64_t)std::max(1.0, std::ceil(dist * safety / target));
+                const uint64_t Si = 1ull << pl.log_s;
+                pl.F = (uint32_t)std::min<uint64_t>(MAX_FINE, std::max<uint64_t>(1, (Pi + Si - 1) / Si));
+                pl.fine_base = (uint32_t)fb;
+                fb += Si * pl.F;
+                if (fb > 0x7fffffffULL) return BATCH_FALLBACK;
+            }
+            P = (uint32_t)fb;
+        } else {
+            for (uint32_t g = 0; g < S; g++) scount[g] = (uint32_t)(soff[g + 1] - soff[g]);
+        }
+        for (uint32_t i = 0; i < n; i++) {
+            const SamplePlan &pl = plans[i];
+            for (uint32_t q = 0; q < (1u << pl.log_s); q++)
+                sinfo[pl.super_base + q] = SuperInfo{pl.fine_base + q * pl.F, pl.F, pl.log_s, 0};
+        }
+        // CHUNK-sized pieces of every super bucket's occurrences
+        std::vector<ulonglong2> chunks;
+        chunks.reserve(n_occ / CHUNK + S + 1);
+        unsigned long long placed = 0;
+        for (uint32_t g = 0; g < S; g++) {
+            placed += scount[g];
+            for (unsigned long long st = 0; st < scount[g]; st += CHUNK) {
+                const unsigned long long len = std::min<unsigned long long>(CHUNK, scount[g] - st);
+                chunks.push_back(make_ulonglong2(soff[g] + st, ((unsigned long long)g << 32) | len));
+            }
+        }
+        if (placed != n_occ) return GX_ECUDA;
+        const uint32_t n_chunks = (uint32_t)chunks.size();
+        if ((e = tar.alloc(okey2_b, n_occ * kb)) != GX_OK) return e;
+        if ((e = tar.alloc(obits2, n_occ)) != GX_OK) return e;
+        if ((e = tar.alloc(d_chunks, std::max<uint32_t>(n_chunks, 1))) != GX_OK) return e;
         if ((e = tar.alloc(fine_cnt, P)) != GX_OK) return e;
         if ((e = tar.alloc(fine_off, P + 1)) != GX_OK) return e;
         if ((e = tar.alloc(fine_cur, P)) != GX_OK) return e;
@@ -272,25 +355,21 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         if ((e = tar.alloc(part_nodes, P)) != GX_OK) return e;
         if ((e = tar.alloc(part_bytes, P)) != GX_OK) return e;
         if ((e = tar.alloc(pscratch, scan_scratch_bytes(P + 1, 8))) != GX_OK) return e;
-        if ((e = tar.alloc(d_plan, n)) != GX_OK) return e;
         if ((e = tar.alloc(d_sinfo, S)) != GX_OK) return e;
         unsigned long long *part_off = nullptr;
         if ((e = tar.alloc(part_off, P + 1)) != GX_OK) return e;
-        void *okey = okey_b, *okey2 = okey2_b;
+        void *okey2 = okey2_b;
         CK(cudaMemcpyAsync(d_plan, plans.data(), n * sizeof(SamplePlan), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(d_sinfo, sinfo.data(), S * sizeof(SuperInfo), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(d_soff, soff.data(), (S + 1) * 8ull, cudaMemcpyHostToDevice, s));
         if (n_chunks)
             CK(cudaMemcpyAsync(d_chunks, chunks.data(), n_chunks * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
-        CK(cudaMemsetAsync(s_cur, 0, S * 4ull, s));
         CK(cudaMemsetAsync(fine_cnt, 0, P * 8ull, s));
         CK(cudaMemsetAsync(fine_cur, 0, P * 4ull, s));
         CK(cudaMemsetAsync(head_cnt, 0, P * 4ull, s));
         CK(cudaMemsetAsync(head_cur, 0, P * 4ull, s));
-        const SampleMap smap{read_base, d_plan, n};
-        CK(cudaEventRecord(tm.ev[2], s));
-        launch_scatter_super(wide, text, n_text, lines, reads, n_reads, k, smap, S, d_soff, s_cur, okey, obits,
-                             0xffffffffu, nullptr, nullptr, s, (uint32_t)jobs[0]->eff_threads_per_read);
+        if (counted)
+            launch_scatter_super(wide, text, n_text, lines, reads, n_reads, k, smap, S, d_soff, s_cur, okey, obits,
+                                 0xffffffffu, nullptr, nullptr, s, tpr);
         launch_heads_part(wide, text, n_text, lines, reads, n_reads, k, smap, heads, head_cnt, s);
         exclusive_scan_u32(head_cnt, head_off, P, nullptr, pscratch, s);
         launch_head_scatter_part(heads, reads, lines, n_reads, head_off, head_cur, head_idx, hsorted, s);
@@ -415,6 +494,7 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
             st.table_partitions = Pi;
             st.attempts = (uint64_t)attempt + 1;
             st.table_slots = (uint64_t)Pi * AGG_SLOTS;
+            st.super_counted = counted ? 1 : 0;  // batch-wide
             st.cov_inexact_nodes = hs.cov_inexact;  // batch-wide
             st.kernel_launches = launches;         // the whole batch's launches
             st.ms_parse = ms_parse;

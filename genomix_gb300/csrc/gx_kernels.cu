@@ -112,6 +112,11 @@ __device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int s
     return ((unsigned long long)hi << 32) | lo;
 }
 
+__device__ __forceinline__ unsigned long long shfl64_up(unsigned long long v, int d) {
+    const uint32_t lo = __shfl_up_sync(0xffffffffu, (uint32_t)v, d), hi = __shfl_up_sync(0xffffffffu, (uint32_t)(v >> 32), d);
+    return ((unsigned long long)hi << 32) | lo;
+}
+
 // Block-wide exclusive scan of one value per thread; ws must hold 33 T.  All threads call.
 template <class T>
 __device__ __forceinline__ T block_exclusive_scan(T v, T *ws, T &total) {
@@ -1641,6 +1646,44 @@ void launch_sample_bounds(const unsigned long long *text_base, uint32_t n_sample
                                                                 nvalid_total, line_base, read_base);
 }
 
+// Occurrences of every sample: each thread its read's L - k + 1, summed over the runs of one
+// sample inside the warp (reads are in sample order), one atomic per run.
+__global__ void k_sample_occ(const LineRec *lines, const uint32_t *reads, int k, SampleMap m,
+                             unsigned long long *occ) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n_reads = m.read_base[m.n];  // the grid covers an upper bound
+    unsigned long long v = 0;
+    uint32_t smp = 0xffffffffu;
+    if (r < n_reads) {
+        const uint32_t rl = reads[r];
+        const LineRec lr = lines[rl >> 1];
+        v = (rl & 1u ? lr.l1 : lr.l0) - (uint32_t)k + 1;
+        smp = sample_of_read(m, r);
+    }
+    unsigned long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = shfl64_up(inc, o);
+        if (lane >= o) inc += y;
+    }
+    const uint32_t s_next = __shfl_down_sync(full, smp, 1);
+    const bool end = lane == 31 || s_next != smp;
+    const uint32_t ends = __ballot_sync(full, end);
+    const uint32_t below = ends & ((1u << lane) - 1u);
+    const int pe = below ? 31 - __clz(below) : 0;
+    const unsigned long long before = shfl64(inc, pe);
+    if (end && smp != 0xffffffffu) atomicAdd(&occ[smp], inc - (below ? before : 0ull));
+}
+
+void launch_sample_occ(const LineRec *lines, const uint32_t *reads, uint32_t n_reads_max, int k, SampleMap m,
+                       unsigned long long *occ, cudaStream_t s) {
+    if (!n_reads_max) return;
+    t_launches++;
+    k_sample_occ<<<(n_reads_max + 255) / 256, 256, 0, s>>>(lines, reads, k, m, occ);
+}
+
 // ---- A2 -------------------------------------------------------------------------------------
 // A round's k-mers stay in registers between counting and placing them (ten per thread; the
 // 128-bit walk, done twice, cost more than the registers of its cache).
@@ -1698,13 +1741,19 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
     // The super buckets this CTA can reach: its reads lie in a run of consecutive samples, which
     // own a contiguous range of buckets (a plain job: all of them).  The per-round loops below
     // cover that range only, so a batch of many samples pays for its own samples' buckets.
-    uint32_t lo = 0, hi = S;
+    uint32_t lo = 0, hi = S, sa = 0, sb = 0;
     if (m.n > 1) {
         const uint32_t ra = blockIdx.x * per_cta, rb = min(n_reads, ra + per_cta) - 1;
-        const SamplePlan pa = m.plan[sample_of_read(m, ra)], pb = m.plan[sample_of_read(m, rb)];
+        sa = sample_of_read(m, ra);
+        sb = sample_of_read(m, rb);
+        const SamplePlan pa = m.plan[sa], pb = m.plan[sb];
         lo = pa.super_base;
         hi = pb.super_base + (1u << pb.log_s);
     }
+    // HyperLogLog registers: SC_HLL_REGS per sample at hll + sample * SC_HLL_REGS, gathered in
+    // shared memory when the CTA's reads are of one sample (nearly always), else directly
+    const uint32_t my_s = (m.n > 1 && r < n_reads) ? sample_of_read(m, r) : 0u;
+    const bool hll_smem = sa == sb;
     if (threadIdx.x == 0) sm.rounds = 0;
     if (hll)
         for (uint32_t i = threadIdx.x; i < SC_HLL_REGS; i += blockDim.x) sm.hll[i] = 0;
@@ -1732,7 +1781,10 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
             if (hll) {
                 const uint64_t w2 = h >> 9;  // HyperLogLog: register = low 9 bits, rank of the rest
                 const uint32_t rho = w2 ? (uint32_t)(__clzll(w2) - 8) : 56u;
-                atomicMax(&sm.hll[h & (SC_HLL_REGS - 1)], rho);
+                if (hll_smem)
+                    atomicMax(&sm.hll[h & (SC_HLL_REGS - 1)], rho);
+                else
+                    atomicMax(&hll[(size_t)my_s * SC_HLL_REGS + (h & (SC_HLL_REGS - 1))], rho);
             }
             if (CACHE) {
                 ck[q] = c;
@@ -1744,7 +1796,8 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
             const uint32_t c = sm_cur[i];
             sm_loff[i] = c;
             uint32_t g = c ? atomicAdd(&s_cur[i], c) : 0u;
-            if (c && (unsigned long long)g + c > cap) {  // the bucket's room is used up: nothing of it is written
+            const unsigned long long room = cap ? (unsigned long long)cap : s_off[i + 1] - s_off[i];
+            if (c && (unsigned long long)g + c > room) {  // the bucket's room is used up: nothing of it is written
                 atomicOr(ovf, 1u);
                 g = 0xffffffffu;
             }
@@ -1796,9 +1849,9 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
         }
         __syncthreads();
     }
-    if (hll)
+    if (hll && hll_smem)
         for (uint32_t i = threadIdx.x; i < SC_HLL_REGS; i += blockDim.x)
-            if (sm.hll[i]) atomicMax(&hll[i], sm.hll[i]);
+            if (sm.hll[i]) atomicMax(&hll[(size_t)sa * SC_HLL_REGS + i], sm.hll[i]);
 }
 
 void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,

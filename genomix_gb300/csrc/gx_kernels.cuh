@@ -156,6 +156,12 @@ void launch_count_occ_batch(int wide, const uint8_t *text, uint64_t n_text, cons
 void launch_sample_bounds(const unsigned long long *text_base, uint32_t n_samples,
                           const unsigned long long *line_end, uint32_t n_lines, const uint32_t *nvalid,
                           const uint32_t *nvalid_total, uint32_t *line_base, uint32_t *read_base, cudaStream_t s);
+// Occurrences (L - k + 1 summed over its reads) of every sample, added into occ[sample]; the
+// reads are m.read_base[m.n] (on the device), at most n_reads_max.
+void launch_sample_occ(const LineRec *lines, const uint32_t *reads, uint32_t n_reads_max, int k, SampleMap m,
+                       unsigned long long *occ, cudaStream_t s);
+// The super scatter.  cap: room per super bucket (0: s_off[i + 1] - s_off[i]); a bucket out of
+// room sets *ovf and is not written.  hll (may be null): SC_HLL_REGS registers per sample.
 void launch_scatter_super(int wide, const uint8_t *text, uint64_t n_text, const LineRec *lines,
                           const uint32_t *reads, uint32_t n_reads, int k, SampleMap m, uint32_t n_super,
                           const unsigned long long *s_off, uint32_t *s_cur, void *okey, uint16_t *obits,

@@ -146,3 +146,33 @@ def test_batch_jobs_outlive_each_other(ctx):
     jobs[0].close()
     same_graph(jobs[2].records(), go.build_graph(texts[2], 21).records)
     jobs[2].close()
+
+
+def test_batch_hot_bucket_falls_back_to_counting(ctx):
+    """A batch scatters without counting first; a sample made of 100,000 copies of one read
+    crowds a few super buckets past their room, so the batch counts its samples and scatters
+    again into exact offsets.  Every sample still equals its plain build and the oracle."""
+    import random
+    rnd = random.Random(5)
+    read = "".join(rnd.choice("ACGT") for _ in range(100))
+    hot = "".join(f"{i}\t{read}\n" for i in range(100_000)).encode()
+    items = [(synth.small_random(600 + i, 800, 100, 31, genome_len=4000, err=0.01), 31) for i in range(3)]
+    items.insert(1, (hot, 31))
+    out = batch(ctx, items)
+    assert out[1][2]["super_counted"] == 1
+    for (text, k), (st, rec, _) in zip(items, out):
+        assert st == 0
+        want, _ = solo(ctx, text, k)
+        assert go.normalize(rec) == go.normalize(want)
+    ref = go.build_graph(hot, 31, threads=8, parts=1)
+    assert go.normalize(out[1][1]) == go.normalize(ref.records)
+
+
+@pytest.mark.parametrize("tpr", [1, 4])
+def test_batch_split_read_walk(ctx, tpr):
+    items = [(synth.small_random(700 + i, 600 + 200 * i, 150, 31, genome_len=3000 + 1000 * i, err=0.01), 31)
+             for i in range(5)]
+    for (text, k), (st, rec, stats) in zip(items, batch(ctx, items, threads_per_read=tpr)):
+        assert st == 0 and stats["super_counted"] == 0  # no counting pass
+        ref = go.build_graph(text, k, threads=4, parts=2)
+        assert go.normalize(rec) == go.normalize(ref.records)
