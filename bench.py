@@ -287,14 +287,20 @@ def bench_serving(ctx, works, rates=SERVE_RATES, n_req=SERVE_REQUESTS):
             for th in ths:
                 th.start()
             lat, kmers, t_end = [], 0, t0
-            lat_small, lat_large = [], []
+            lat_small, lat_large, srv_small, cli_small = [], [], [], []
             for i in range(n_req):
                 ready[i].wait()
                 st, srv_ms = srv.poll(tickets[i])
                 assert st == 0, st
-                lt = (t_sub[i] - (t0 + arr[i])) * 1e3 + srv_ms  # arrival -> done
+                cli_ms = (t_sub[i] - (t0 + arr[i])) * 1e3  # arrival -> submitted (job made, input copied)
+                lt = cli_ms + srv_ms  # arrival -> done
                 lat.append(lt)
-                (lat_small if len(works[i % len(works)].text) <= median_bytes else lat_large).append(lt)
+                if len(works[i % len(works)].text) <= median_bytes:
+                    lat_small.append(lt)
+                    srv_small.append(srv_ms)
+                    cli_small.append(cli_ms)
+                else:
+                    lat_large.append(lt)
                 t_end = max(t_end, t0 + arr[i] + lt / 1e3)
                 kmers += jobs[i].stats()["kmers"]
                 jobs[i].close()
@@ -304,7 +310,8 @@ def bench_serving(ctx, works, rates=SERVE_RATES, n_req=SERVE_REQUESTS):
             out.append({"offered_jobs_per_s": rate, "jobs": n_req, "achieved_jobs_per_s": n_req / span,
                         "kmers_per_s": kmers / span, "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99),
                         "p50_small_ms": pct(lat_small, 0.5), "p99_small_ms": pct(lat_small, 0.99),
-                        "p50_large_ms": pct(lat_large, 0.5), "p99_large_ms": pct(lat_large, 0.99)})
+                        "p50_large_ms": pct(lat_large, 0.5), "p99_large_ms": pct(lat_large, 0.99),
+                        "p99_small_server_ms": pct(srv_small, 0.99), "p99_small_client_ms": pct(cli_small, 0.99)})
         st = srv.stats()
     for p in pins:
         p.close()
@@ -487,7 +494,8 @@ def compact_serving(srv):
     if not srv:
         return srv
     out = {k: v for k, v in srv.items() if k != "rates"}
-    cols = ["offered_jobs_per_s", "achieved_jobs_per_s", "p50_ms", "p99_ms", "p99_small_ms", "p99_large_ms"]
+    cols = ["offered_jobs_per_s", "achieved_jobs_per_s", "p50_ms", "p99_ms", "p99_small_ms", "p99_large_ms",
+            "p99_small_server_ms", "p99_small_client_ms"]
     out["rates"] = [[None if r[c] is None else round(r[c], 2) for c in cols] for r in srv["rates"]]
     out["rates_columns"] = cols
     return out
