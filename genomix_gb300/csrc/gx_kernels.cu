@@ -2175,8 +2175,6 @@ struct AggSmem {
     uint32_t wsv[32];
     uint32_t hrank[32];                // kept read heads in order: their node's rank ...
     uint32_t hcum[33];                 // ... and the bytes of the kept heads before each
-    K mq_key[8][64];                   // per warp: occurrences waiting for the probe ...
-    uint16_t mq_bits[8][64];           // ... and their edge bits
     unsigned long long carry;
     uint32_t n, fail, kept, base_total;
 };
@@ -2326,29 +2324,6 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             a.heads[r].slot = (uint32_t)sl;
         }
     }
-    // Occurrences whose key is not in its home slot (a key's first sighting, or one that probed
-    // past its home) wait in a per-warp queue and are inserted 32 at a time: the probe loop then
-    // runs with full warps, not once for every few occurrences of every warp.
-    K *const mq_key = sm.mq_key[warp];
-    uint16_t *const mq_bits = sm.mq_bits[warp];
-    uint32_t qn = 0;  // queued entries (the same in every lane)
-    auto drain = [&](uint32_t cnt) {  // inserts entries [0, cnt), cnt <= 32
-        __syncwarp();
-        if ((uint32_t)lane < cnt) {
-            const K key = mq_key[lane];
-            const uint32_t bits = mq_bits[lane];
-            uint32_t claimed = 0;
-            const int sl = AggTable<K>::insert(sm.key1, key, agg_home(key), claimed);
-            if (sl < 0) {
-                sm.fail = 1;
-            } else {
-                if (claimed) atomicAdd(&sm.n, 1u);
-                atomicAdd(&sm.cnt[sl], 1u);
-                if (bits) atomicOr(&sm.meta[sl], bits);
-            }
-        }
-        __syncwarp();
-    };
     for (uint32_t c0 = 0; c0 < M; c0 += BATCH * blockDim.x) {
         if (c0) {
 #pragma unroll
@@ -2359,8 +2334,8 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             }
         }
         // In groups of four: the home slots are read first, all four loads in flight (a key
-        // never leaves the slot it was put in, so a plain read that shows it is final); a hit
-        // is counted at once, a miss joins the queue.
+        // never leaves the slot it was put in, so a plain read that shows it is final); an
+        // occurrence whose key is not in its home slot takes the probe with compare-and-swap.
 #pragma unroll
         for (int g = 0; g < BATCH; g += 4) {
             uint32_t hm[4];
@@ -2373,40 +2348,23 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 const int q = g + u;
-                const bool valid = c0 + q * blockDim.x + threadIdx.x < M;
-                const bool hit = valid && cur[u] == kk[q] + 1;
-                if (hit) {
-                    atomicAdd(&sm.cnt[hm[u]], 1u);  // no result used: both are fire-and-forget reductions
-                    if (bb[q]) atomicOr(&sm.meta[hm[u]], bb[q]);
-                }
-                const uint32_t mm = __ballot_sync(full, valid && !hit);
-                if (valid && !hit) {
-                    const uint32_t pos = qn + __popc(mm & ((1u << lane) - 1u));
-                    mq_key[pos] = kk[q];
-                    mq_bits[pos] = (uint16_t)bb[q];
-                }
-                qn += __popc(mm);
-                if (qn >= 32) {
-                    drain(32);
-                    // the rest (fewer than 32) moves to the front
-                    const bool mv = (uint32_t)lane < qn - 32;
-                    K tk{};
-                    uint16_t tb = 0;
-                    if (mv) {
-                        tk = mq_key[32 + lane];
-                        tb = mq_bits[32 + lane];
+                const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
+                if (i >= M) continue;
+                int sl = (int)hm[u];
+                if (cur[u] != kk[q] + 1) {
+                    uint32_t claimed = 0;
+                    sl = AggTable<K>::insert(sm.key1, kk[q], hm[u], claimed);
+                    if (sl < 0) {
+                        sm.fail = 1;
+                        continue;
                     }
-                    __syncwarp();
-                    if (mv) {
-                        mq_key[lane] = tk;
-                        mq_bits[lane] = tb;
-                    }
-                    qn -= 32;
+                    if (claimed) atomicAdd(&sm.n, 1u);
                 }
+                atomicAdd(&sm.cnt[sl], 1u);  // no result used: both are fire-and-forget reductions
+                if (bb[q]) atomicOr(&sm.meta[sl], bb[q]);
             }
         }
     }
-    if (qn) drain(qn);
     __syncthreads();
     const uint32_t n = sm.n;
     if (sm.fail || n >= AGG_SLOTS) {  // the ordering below needs an empty slot
