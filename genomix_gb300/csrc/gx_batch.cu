@@ -431,6 +431,7 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         a.g = TableGeom{nullptr, P, wide};
         a.k = k;
         a.text = text;
+        a.n_text = n_text;
         a.lines = lines;
         a.reads = reads;
         a.heads = heads;
@@ -450,6 +451,7 @@ gx_status run_group_impl(gx_ctx *c, const std::vector<gx_job *> &jobs) {
         a.noff = noff;
         a.hout = hout;
         a.n_head_slots = n_reads;
+        a.max_seq = hs.max_seq;
         CK(cudaEventRecord(tm.ev[5], s));
         launch_emit_write_part(a, s);
         CK(cudaEventRecord(tm.ev[6], s));

@@ -39,7 +39,7 @@ struct DevStatus {
     unsigned int big_head_parts;   // partitions whose read heads exceeded the in-CTA sort
     unsigned int cov_inexact;      // nodes with count >= 2^24
     unsigned int internal_err;     // emission size check failed (never expected)
-    unsigned int pad;
+    unsigned int max_seq;          // longest read or mate sequence of a kept read head (letters)
 };
 
 // ---- bases ------------------------------------------------------------------------------

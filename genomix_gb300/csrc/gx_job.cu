@@ -730,6 +730,7 @@ static gx_status build_table(RunCtx &rc) {
         a.g = g;
         a.k = k;
         a.text = rc.text;
+        a.n_text = rc.n_text;
         a.lines = rc.lines;
         a.reads = rc.reads;
         a.heads = heads;
@@ -1121,6 +1122,7 @@ static gx_status build_partitioned(RunCtx &rc) {
         a.g = TableGeom{nullptr, P, wide};
         a.k = k;
         a.text = rc.text;
+        a.n_text = rc.n_text;
         a.lines = rc.lines;
         a.reads = rc.reads;
         a.heads = heads;
@@ -1140,6 +1142,7 @@ static gx_status build_partitioned(RunCtx &rc) {
         a.noff = noff;
         a.hout = hout;
         a.n_head_slots = n_reads;
+        a.max_seq = hs.max_seq;
         CK(cudaEventRecord(tm.ev[5], s));
         launch_emit_write_part(a, s);
         CK(cudaEventRecord(tm.ev[6], s));

@@ -2499,6 +2499,8 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             wkeep_mask = __ballot_sync(full, wkeep);
             wkept_idx = __popc(wkeep_mask & ((1u << lane) - 1u));
             hsz = wkeep ? 1 + 8 + 4 + packed_len(w_L) + (w_Lm > 0 ? 4 + packed_len(w_Lm) : 0) : 0u;
+            const uint32_t longest = __reduce_max_sync(full, wkeep ? max(w_L, w_Lm) : 0u);
+            if (lane == 0 && longest) atomicMax(&a.st->max_seq, longest);
             const uint32_t incl = warp_inclusive_scan(hsz);
             const uint32_t kept_w = __popc(wkeep_mask);
             // kept heads in order: node rank and the bytes of the kept heads before
@@ -2686,6 +2688,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
         ho.m_off = mate ? lr.s0 : lr.s1;
         ho.L = mate ? lr.l1 : lr.l0;
         ho.Lm = mate ? lr.l0 : lr.l1;
+        atomicMax(&a.st->max_seq, max(ho.L, ho.Lm));
         ho.pos = pos;
         ho.set_count = (i == st && !flipped) ? cu : ((flipped && i == st + cu) ? cf : 0u);
         ho.part = f;
@@ -2834,91 +2837,246 @@ __device__ __forceinline__ uint32_t pack4_letters(uint32_t w) {
     return (y | (y >> 12)) & 0xFFu;
 }
 
-// One read head and, on the first head of a set, the set's header: each lane writes one header
-// byte and two packed bytes of each sequence, every letter of both sequences loaded before any
-// byte is stored.  Sequences longer than 256 letters take the byte-at-a-time path.
-__device__ __forceinline__ void write_head(const Sink &ow, long long hp, uint32_t L, uint32_t Lm, uint32_t setc,
-                                           unsigned long long uuid, const uint8_t *s, const uint8_t *m, int lane) {
-    const uint32_t nbr = packed_len(L), nbm = packed_len(Lm);
-    // header bytes, one lane each: [set flag, set count], flags, uuid, L, and Lm after the read
-    bool put = false;
-    long long at = 0;
-    uint32_t v = 0;
-    if (lane < 5) {
-        put = setc != 0;  // ExternalableTreeSet: whole body in stream, then the count
-        at = hp - 5 + lane;
-        v = lane == 0 ? 1u : (setc >> (8 * (4 - lane))) & 0xffu;
-    } else if (lane == 5) {
-        put = true;
-        at = hp;
-        v = Lm ? 1u : 0u;
-    } else if (lane < 14) {
-        put = true;
-        at = hp + 1 + (lane - 6);
-        v = (uint32_t)(uuid >> (8 * (13 - lane))) & 0xffu;
-    } else if (lane < 18) {
-        put = true;
-        at = hp + 9 + (lane - 14);
-        v = (L >> (8 * (17 - lane))) & 0xffu;
-    } else if (lane < 22) {
-        put = Lm != 0;
-        at = hp + 13 + nbr + (lane - 18);
-        v = (Lm >> (8 * (21 - lane))) & 0xffu;
+// Bytes appended to global memory in address order: whole aligned 32-bit words inside the run,
+// single bytes in its first and last word, which it may share with its neighbours' bytes.
+struct ByteRun {
+    uint8_t *out;
+    unsigned long long wa;  // address of the word being filled (a multiple of 4)
+    uint32_t lo;            // first byte of that word inside the run (nonzero only in the first word)
+    uint32_t fill;          // bytes of that word filled so far (lo <= fill < 4)
+    uint32_t cur;           // their values: byte b of the word in bits 8b .. 8b + 7
+    __device__ __forceinline__ void init(uint8_t *o, unsigned long long pos) {
+        out = o;
+        wa = pos & ~3ULL;
+        lo = fill = (uint32_t)(pos & 3);
+        cur = 0;
     }
-    if (put) ow.b(at, v);
-    // the packed bytes of both sequences as one run of nbr + nbm, 128 at a time: byte t < nbr is
-    // read byte t, the rest mate bytes; byte j of a sequence holds letters 4 (nb - 1 - j) + 0..3
-    const uint32_t tot = nbr + nbm;
-    for (uint32_t t0 = 0; t0 < tot; t0 += 128) {
-        uint32_t w[4];
-#pragma unroll
-        for (int it = 0; it < 4; it++) {
-            const uint32_t t = t0 + (uint32_t)lane + 32u * it;
-            const bool mate = t >= nbr;
-            const uint8_t *q = mate ? m : s;
-            const uint32_t len = mate ? Lm : L, j = mate ? t - nbr : t;
-            const uint32_t i0 = 4 * ((mate ? nbm : nbr) - 1 - j);
-            uint32_t x = 0;
-            if (t < tot) {
-#pragma unroll
-                for (int c = 0; c < 4; c++)
-                    if (i0 + c < len) x |= (uint32_t)q[i0 + c] << (8 * c);
-            }
-            w[it] = x;
+    __device__ __forceinline__ void word_out(uint32_t v) {
+        if (lo == 0) {
+            *reinterpret_cast<uint32_t *>(out + wa) = v;
+        } else {
+            for (uint32_t b = lo; b < 4; b++) out[wa + b] = (uint8_t)(v >> (8 * b));
+            lo = 0;
         }
+    }
+    // n (1..4) bytes, the first in the low byte of le, the bytes above n zero
+    __device__ __forceinline__ void put(uint32_t le, uint32_t n) {
+        const uint32_t sh = fill * 8;
+        const uint32_t v = cur | (le << sh);
+        fill += n;
+        if (fill >= 4) {
+            word_out(v);
+            wa += 4;
+            fill -= 4;
+            cur = __funnelshift_rc(le, 0u, 32 - sh);  // the bytes that spill into the next word
+        } else {
+            cur = v;
+        }
+    }
+    __device__ __forceinline__ void finish() {
+        for (uint32_t b = lo; b < fill; b++) out[wa + b] = (uint8_t)(cur >> (8 * b));
+    }
+};
+
+__device__ __forceinline__ uint32_t bswap32(uint32_t v) { return __byte_perm(v, 0, 0x0123); }
+
+// The aligned 16 bytes at address c as four little-endian words; bytes outside the text
+// [text, text + n_text) read as 0 (only the text's first and last 16 bytes take the byte loop).
+__device__ __forceinline__ uint4 text_chunk(const uint8_t *text, unsigned long long n_text, uintptr_t c) {
+    const uintptr_t tb = (uintptr_t)text, te = tb + n_text;
+    if (c >= tb && c + 16 <= te) return *reinterpret_cast<const uint4 *>(c);
+    uint32_t w[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-        for (int it = 0; it < 4; it++) {
-            const uint32_t t = t0 + (uint32_t)lane + 32u * it;
-            if (t < tot) ow.b(t < nbr ? hp + 13 + t : hp + 17 + t, pack4_letters(w[it]));
+    for (int b = 0; b < 16; b++)
+        if (c + b >= tb && c + b < te) w[b >> 2] |= (uint32_t)*reinterpret_cast<const uint8_t *>(c + b) << (8 * (b & 3));
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// the 16 bytes starting o (0..15) bytes into the 32 bytes lo, hi, as four little-endian words
+__device__ __forceinline__ void realign16(const uint4 &lo, const uint4 &hi, uint32_t o, uint32_t v[4]) {
+    const uint32_t q = o >> 2, sh = (o & 3u) * 8u;
+    const uint32_t e0 = q == 0 ? lo.x : q == 1 ? lo.y : q == 2 ? lo.z : lo.w;
+    const uint32_t e1 = q == 0 ? lo.y : q == 1 ? lo.z : q == 2 ? lo.w : hi.x;
+    const uint32_t e2 = q == 0 ? lo.z : q == 1 ? lo.w : q == 2 ? hi.x : hi.y;
+    const uint32_t e3 = q == 0 ? lo.w : q == 1 ? hi.x : q == 2 ? hi.y : hi.z;
+    const uint32_t e4 = q == 0 ? hi.x : q == 1 ? hi.y : q == 2 ? hi.z : hi.w;
+    v[0] = __funnelshift_r(e0, e1, sh);
+    v[1] = __funnelshift_r(e1, e2, sh);
+    v[2] = __funnelshift_r(e2, e3, sh);
+    v[3] = __funnelshift_r(e3, e4, sh);
+}
+
+// 16-byte chunks of the text read straight from global memory (bytes outside the text as 0)
+struct TextChunks {
+    const uint8_t *text;
+    unsigned long long n_text;
+    __device__ __forceinline__ uint4 get(uintptr_t c) const { return text_chunk(text, n_text, c); }
+};
+// the same chunks from a copy in shared memory of the chunks [c0, c0 + 16 n)
+struct StagedChunks {
+    const uint4 *s;
+    uintptr_t c0;
+    __device__ __forceinline__ uint4 get(uintptr_t c) const { return s[(c - c0) >> 4]; }
+};
+
+// The packed letters of a sequence of L letters at address a (VKmer.setAsCopy(String),
+// VKmer.java:450-479): nb = ceil(L / 4) bytes, byte j holding letters 4 (nb - 1 - j) .. + 3, the
+// first in the low bits, letters past L as 0.  Four bytes per step, from the 16 letters at
+// a + 4 nb - 16 - 16 s: the sequence is read backwards, one aligned 16-byte chunk per step.  The
+// windows start at most 12 bytes before the sequence (letters of groups before its first,
+// never written); the chunks they touch are [floor16(a - 12), floor16(a + 4 nb) + 16).
+// Four letters known to be in [ACGTacgt] (or 0 bytes past the sequence's end) packed the same
+// way: (b >> 1) & 3 gives A 0, C 1, G 3, T 2 in both cases, bit 2 of the letter swaps G and T.
+__device__ __forceinline__ uint32_t pack4_acgt(uint32_t w) {
+    const uint32_t c = ((w >> 1) & 0x03030303u) ^ ((w >> 2) & 0x01010101u);
+    const uint32_t y = c | (c >> 6);
+    return (y | (y >> 12)) & 0xFFu;
+}
+template <bool ACGT>
+__device__ __forceinline__ uint32_t pack4(uint32_t w) {
+    return ACGT ? pack4_acgt(w) : pack4_letters(w);
+}
+
+template <bool ACGT, class Run, class Src>
+__device__ __forceinline__ void put_packed_seq(Run &o, const Src &src, uintptr_t a, uint32_t L) {
+    const uint32_t nb = packed_len(L);
+    if (!nb) return;
+    const uintptr_t a0 = a + 4ull * nb - 16ull;
+    const uint32_t off = (uint32_t)(a0 & 15u);
+    uintptr_t c = a0 & ~(uintptr_t)15;
+    uint4 hi = src.get(c + 16), lo = src.get(c);
+    const uint32_t tail = L - 4 * (nb - 1);  // letters of the last group (1..4)
+    const uint32_t tail_mask = tail >= 4 ? 0xffffffffu : (1u << (8 * tail)) - 1u;
+    for (uint32_t j0 = 0; j0 < nb; j0 += 4) {
+        uint32_t v[4];
+        realign16(lo, hi, off, v);
+        if (j0 == 0) v[3] &= tail_mask;
+        const uint32_t n = min(4u, nb - j0);
+        uint32_t w = pack4<ACGT>(v[3]);
+        if (n > 1) w |= pack4<ACGT>(v[2]) << 8;
+        if (n > 2) w |= pack4<ACGT>(v[1]) << 16;
+        if (n > 3) w |= pack4<ACGT>(v[0]) << 24;
+        o.put(w, n);
+        if (j0 + 4 < nb) {
+            c -= 16;
+            hi = lo;
+            lo = src.get(c);
         }
     }
 }
 
+// bytes of one read head, with the set header ahead of a set's first head
+__device__ __forceinline__ uint32_t head_out_bytes(const HeadOut &h) {
+    return (h.set_count ? 5u : 0u) + 1u + 8u + 4u + packed_len(h.L) + (h.Lm ? 4u + packed_len(h.Lm) : 0u);
+}
+
+__device__ __forceinline__ void cp_async16(void *dst_smem, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst_smem)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// The chunks a sequence's packing reads: [floor16(a - 12), floor16(a + 4 nb) + 16).
+__device__ __forceinline__ uintptr_t seq_chunk0(uintptr_t a) { return (a - 12) & ~(uintptr_t)15; }
+__device__ __forceinline__ uint32_t seq_chunks(uintptr_t a, uint32_t L) {
+    return L ? (uint32_t)(((((a + 4ull * packed_len(L)) & ~(uintptr_t)15) + 16) - seq_chunk0(a)) >> 4) : 0u;
+}
+
+// Warp-collective: each lane's sequence (where `want`) into the lane's slot of `slots` (seqc
+// chunks per lane), one sequence after another, a chunk per lane, by asynchronous copies (the
+// text's first and last chunk, which may reach past it, by plain loads).
+__device__ __forceinline__ void stage_seqs(uint4 *slots, uint32_t seqc, bool want, uintptr_t a, uint32_t L,
+                                           const uint8_t *text, unsigned long long n_text, int lane) {
+    const unsigned full = 0xffffffffu;
+    const uintptr_t tb = (uintptr_t)text, te = tb + n_text;
+    uint32_t pend = __ballot_sync(full, want);
+    while (pend) {
+        const int q = __ffs(pend) - 1;
+        pend &= pend - 1;
+        const uintptr_t aq = (uintptr_t)shfl64((unsigned long long)a, q);
+        const uint32_t Lq = __shfl_sync(full, L, q);
+        const uint32_t j = (uint32_t)lane;
+        if (j < seq_chunks(aq, Lq)) {  // at most seqc <= 31: `want` is only set when it fits
+            const uintptr_t c = seq_chunk0(aq) + 16ull * j;
+            uint4 *dst = slots + (size_t)q * seqc + j;
+            if (c >= tb && c + 16 <= te)
+                cp_async16(dst, reinterpret_cast<const void *>(c));
+            else
+                *dst = text_chunk(text, n_text, c);
+        }
+    }
+    cp_async_wait_all();
+    __syncwarp();
+}
+
 // The read-head sets of the partitioned build, straight into the record stream after the record
 // writer: the writer leaves those byte ranges to this kernel (it copies whatever its window held
-// there).  A warp takes 32 head slots at a time: lane h loads slot h and its partition's offset,
-// then the warp writes the heads one after another; slots of dropped duplicates are skipped.
-__global__ void __launch_bounds__(256) k_write_heads_part(const HeadOut *hout, uint64_t n,
-                                                          const unsigned long long *part_off, const uint8_t *text,
-                                                          uint8_t *out) {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const Sink o{out, 0, 0, true};
-    for (uint64_t h0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; h0 < n; h0 += nw * 32) {
-        const uint32_t nh = n - h0 < 32 ? (uint32_t)(n - h0) : 32u;
-        HeadOut mine{};
-        mine.part = HEAD_DROPPED;
-        if ((uint32_t)lane < nh) mine = hout[h0 + lane];
-        const unsigned long long hp = mine.part != HEAD_DROPPED ? part_off[mine.part] + mine.pos : 0ull;
-        uint32_t live = __ballot_sync(full, mine.part != HEAD_DROPPED);
-        while (live) {
-            const int q = __ffs(live) - 1;
-            live &= live - 1;
-            write_head(o, (long long)shfl64(hp, q), __shfl_sync(full, mine.L, q), __shfl_sync(full, mine.Lm, q),
-                       __shfl_sync(full, mine.set_count, q), shfl64(mine.uuid, q), text + shfl64(mine.s_off, q),
-                       text + shfl64(mine.m_off, q), lane);
+// there).  A warp takes 32 head slots at a time, one per lane (slots of dropped duplicates are
+// skipped); each lane writes its head in order: on a set's first head the set header
+// (ExternalableTreeSet.write: [1, set count]), then ReadHeadInfo.write: a mate flag, the uuid,
+// the read's length and letters, the mate's length and letters when it has one.  The letters
+// come through shared memory: the warp copies the 16-byte chunks of its 32 reads, one read after
+// another and a chunk per lane, so the loads are coalesced and in flight together; the lanes
+// pack their reads from there; then the same for the mates.  seqc (odd, so the lanes' slots
+// start in different bank groups) is the chunks of the longest sequence; a sequence that needs
+// more (or every one, when seqc is 0) is read straight from global memory.  A head's own read
+// matched [ACGTacgt]+ in the parse, so it packs with the shorter letter code; the mate may hold
+// any letter.
+constexpr int HEAD_WARPS = 4;
+constexpr uint32_t HEAD_MAX_SEQ_CHUNKS = 31;
+
+__global__ void __launch_bounds__(HEAD_WARPS * 32) k_write_heads_part(const HeadOut *hout, uint64_t n,
+                                                                      const unsigned long long *part_off,
+                                                                      const uint8_t *text, unsigned long long n_text,
+                                                                      uint8_t *out, uint32_t seqc) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint4 *slots = reinterpret_cast<uint4 *>(smem_raw) + (size_t)warp * 32 * seqc;
+    const uint4 *mine = slots + (size_t)lane * seqc;
+    const uintptr_t tb = (uintptr_t)text;
+    const TextChunks gsrc{text, n_text};
+    const uint64_t step = (uint64_t)gridDim.x * HEAD_WARPS * 32;
+    for (uint64_t h0 = ((uint64_t)blockIdx.x * HEAD_WARPS + warp) * 32; h0 < n; h0 += step) {
+        const uint64_t i = h0 + lane;
+        HeadOut h{};
+        h.part = HEAD_DROPPED;
+        if (i < n) h = hout[i];
+        const bool live = h.part != HEAD_DROPPED;
+        const uintptr_t ar = tb + h.s_off, am = tb + h.m_off;
+        ByteRun o;
+        if (live) {
+            const unsigned long long hp = part_off[h.part] + h.pos;
+            o.init(out, h.set_count ? hp - 5 : hp);
+            if (h.set_count) {
+                o.put(1u, 1);
+                o.put(bswap32(h.set_count), 4);
+            }
+            o.put(h.Lm ? 1u : 0u, 1);
+            o.put(bswap32((uint32_t)(h.uuid >> 32)), 4);
+            o.put(bswap32((uint32_t)h.uuid), 4);
+            o.put(bswap32(h.L), 4);
         }
+        const bool sr = live && seq_chunks(ar, h.L) <= seqc;
+        stage_seqs(slots, seqc, sr, ar, h.L, text, n_text, lane);
+        if (live) {
+            if (sr)
+                put_packed_seq<true>(o, StagedChunks{mine, seq_chunk0(ar)}, ar, h.L);
+            else
+                put_packed_seq<true>(o, gsrc, ar, h.L);
+            if (h.Lm) o.put(bswap32(h.Lm), 4);
+        }
+        __syncwarp();  // the slots are read before the mates go in
+        const bool sm = live && h.Lm && seq_chunks(am, h.Lm) <= seqc;
+        stage_seqs(slots, seqc, sm, am, h.Lm, text, n_text, lane);
+        if (live) {
+            if (sm)
+                put_packed_seq<false>(o, StagedChunks{mine, seq_chunk0(am)}, am, h.Lm);
+            else if (h.Lm)
+                put_packed_seq<false>(o, gsrc, am, h.Lm);
+            o.finish();
+        }
+        __syncwarp();
     }
 }
 
@@ -3092,8 +3250,14 @@ void launch_emit_write_part(const EmitArgs &a, cudaStream_t s) {
     }
     if (a.n_head_slots) {
         t_launches++;
-        const unsigned blocks = (unsigned)std::min<uint64_t>((a.n_head_slots + 255) / 256, 152ull * 8);
-        k_write_heads_part<<<blocks, 256, 0, s>>>(a.hout, a.n_head_slots, a.part_off, a.text, a.out);
+        // slots of the longest read-head sequence's chunks (odd), when they fit
+        uint32_t seqc = a.max_seq ? ((4u * ((a.max_seq + 3) / 4) + 27) >> 4) + 1 : 13u;
+        seqc |= 1u;
+        if (seqc > HEAD_MAX_SEQ_CHUNKS) seqc = 0;
+        const size_t smem = (size_t)HEAD_WARPS * 32 * seqc * 16;
+        const unsigned blocks = (unsigned)std::min<uint64_t>((a.n_head_slots + HEAD_WARPS * 32 - 1) / (HEAD_WARPS * 32), 152ull * 16);
+        cudaFuncSetAttribute(k_write_heads_part, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_write_heads_part<<<blocks, HEAD_WARPS * 32, smem, s>>>(a.hout, a.n_head_slots, a.part_off, a.text, a.n_text, a.out, seqc);
     }
 }
 

@@ -72,6 +72,7 @@ struct EmitArgs {
     TableGeom g;
     int k;
     const uint8_t *text;
+    uint64_t n_text;             // bytes of text (the head writer reads no byte past them)
     const LineRec *lines;
     const uint32_t *reads;
     Head *heads;
@@ -92,6 +93,7 @@ struct EmitArgs {
     const uint32_t *noff = nullptr;
     const HeadOut *hout = nullptr;
     uint64_t n_head_slots = 0;   // entries of hout: kept heads and dropped duplicates
+    uint32_t max_seq = 0;        // longest sequence of a kept read head (0: not known)
 };
 void launch_emit_prepare(const EmitArgs &a, cudaStream_t s);
 void launch_emit_write(const EmitArgs &a, cudaStream_t s);

@@ -180,6 +180,7 @@ static gx_status build_noalloc(int device, const void *text_dev, size_t n_text, 
         a.g = g;
         a.k = k;
         a.text = text;
+        a.n_text = n_text;
         a.lines = lines;
         a.reads = reads;
         a.heads = heads;
