@@ -1757,15 +1757,15 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
     if (threadIdx.x == 0) sm.rounds = 0;
     if (hll)
         for (uint32_t i = threadIdx.x; i < SC_HLL_REGS; i += blockDim.x) sm.hll[i] = 0;
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) sm_cur[i] = 0;  // then by each round's write-out
     __syncthreads();
     atomicMax(&sm.rounds, (w.jend - w.j + RN - 1) / RN);
     __syncthreads();
     const uint32_t rounds = sm.rounds;
     K ck[CACHE ? RN : 1];
     uint32_t cb[CACHE ? RN : 1];  // edge bits | super << 16
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint32_t round = 0; round < rounds; round++) {
-        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) sm_cur[i] = 0;
-        __syncthreads();
         const Walker<K> w0 = w;
         const uint32_t nq = w.j < w.jend ? min((uint32_t)RN, w.jend - w.j) : 0u;
         // count this round's occurrences per super bucket
@@ -1792,28 +1792,62 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
             }
         }
         __syncthreads();
-        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-            const uint32_t c = sm_cur[i];
-            sm_loff[i] = c;
-            uint32_t g = c ? atomicAdd(&s_cur[i], c) : 0u;
-            const unsigned long long room = cap ? (unsigned long long)cap : s_off[i + 1] - s_off[i];
-            if (c && (unsigned long long)g + c > room) {  // the bucket's room is used up: nothing of it is written
-                atomicOr(ovf, 1u);
-                g = 0xffffffffu;
+        // Each bucket claims its run in global memory (s_cur) and gets its offset in the round's
+        // staging (loff, exclusive).  Element i of bucket sp then goes to s_off[sp] + claim +
+        // (i - loff[sp]): that base is kept as gbase (high word, ~0 for a bucket out of room)
+        // and glo (low word).
+        uint32_t tot;
+        if (hi - lo <= SC_THREADS) {
+            // one bucket per thread: its claim is in flight while the block scans the counts
+            const uint32_t i = lo + threadIdx.x;
+            const bool mine = i < hi;
+            const uint32_t c = mine ? sm_cur[i] : 0u;
+            const uint32_t g = c ? atomicAdd(&s_cur[i], c) : 0u;
+            const uint32_t inc = warp_inclusive_scan(c);
+            if (lane == 31) sm.ws[warp] = inc;
+            __syncthreads();
+            uint32_t before = 0;
+            tot = 0;
+#pragma unroll
+            for (int q = 0; q < SC_THREADS / 32; q++) {
+                const uint32_t x = sm.ws[q];
+                if (q < warp) before += x;
+                tot += x;
             }
-            sm_gbase[i] = g;
-        }
-        __syncthreads();
-        const uint32_t tot = block_scan_array(sm_loff + lo, hi - lo, sm.ws);
-        // element i of bucket sp goes to s_off[sp] + gbase[sp] + (i - loff[sp]): the base, as
-        // gbase (high word, ~0 for a bucket out of room) and glo (low word)
-        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-            sm_cur[i] = 0;
-            const uint32_t g = sm_gbase[i];
-            if (g != 0xffffffffu) {
-                const unsigned long long b = s_off[i] + g - sm_loff[i];
-                sm_glo[i] = (uint32_t)b;
-                sm_gbase[i] = (uint32_t)(b >> 32);
+            if (mine) {
+                const uint32_t ex = before + inc - c;
+                sm_loff[i] = ex;
+                const unsigned long long room = cap ? (unsigned long long)cap : s_off[i + 1] - s_off[i];
+                if (c && (unsigned long long)g + c > room) {  // the bucket's room is used up: nothing of it is written
+                    atomicOr(ovf, 1u);
+                    sm_gbase[i] = 0xffffffffu;
+                } else {
+                    const unsigned long long b = s_off[i] + g - ex;
+                    sm_glo[i] = (uint32_t)b;
+                    sm_gbase[i] = (uint32_t)(b >> 32);
+                }
+            }
+        } else {
+            for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+                const uint32_t c = sm_cur[i];
+                sm_loff[i] = c;
+                uint32_t g = c ? atomicAdd(&s_cur[i], c) : 0u;
+                const unsigned long long room = cap ? (unsigned long long)cap : s_off[i + 1] - s_off[i];
+                if (c && (unsigned long long)g + c > room) {
+                    atomicOr(ovf, 1u);
+                    g = 0xffffffffu;
+                }
+                sm_gbase[i] = g;
+            }
+            __syncthreads();
+            tot = block_scan_array(sm_loff + lo, hi - lo, sm.ws);
+            for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+                const uint32_t g = sm_gbase[i];
+                if (g != 0xffffffffu) {
+                    const unsigned long long b = s_off[i] + g - sm_loff[i];
+                    sm_glo[i] = (uint32_t)b;
+                    sm_gbase[i] = (uint32_t)(b >> 32);
+                }
             }
         }
         __syncthreads();
@@ -1833,13 +1867,14 @@ __global__ void __launch_bounds__(SC_THREADS, sizeof(K) == 8 ? 4 : 2) k_scatter_
                 w.next(c, b, d);
                 sp = sbase + super_local(KeyOps<K>::hash(c), log_s);
             }
-            const uint32_t pos = sm_loff[sp] + atomicAdd(&sm_cur[sp], 1u);
+            const uint32_t pos = atomicAdd(&sm_loff[sp], 1u);  // loff runs through the bucket's staging
             sm.key[pos] = c;
             sm.bits[pos] = (uint16_t)b;
             sm.sup[pos] = (uint16_t)sp;
         }
         __syncthreads();
-        // write the runs out
+        // write the runs out; the counts start from zero for the next round
+        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) sm_cur[i] = 0;
         for (uint32_t i = threadIdx.x; i < tot; i += blockDim.x) {
             const uint32_t sp = sm.sup[i], hi = sm_gbase[sp];
             if (hi == 0xffffffffu) continue;
