@@ -1972,6 +1972,7 @@ void launch_fine_count(int wide, const void *okey, const ulonglong2 *chunks, uin
 }
 
 // ---- B2 -------------------------------------------------------------------------------------
+constexpr int FINE_BOOK = 2;  // fine buckets per thread in the scatter's fast bookkeeping (F <= 512)
 template <class K>
 struct FineSmem {
     K key[CHUNK];
@@ -2019,27 +2020,59 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 3 : 2) k_scatter_fine(co
         if (q * 256 + threadIdx.x < len) atomicAdd(&sm.cur[bkt], 1u);
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) {
-        sm.loff[i] = sm.cur[i];
-        sm.gbase[i] = sm.cur[i] ? atomicAdd(&fine_cur[f0 + i], sm.cur[i]) : 0u;
-    }
-    __syncthreads();
-    block_scan_array(sm.loff, F, sm.ws);
-    // Element i of bucket b (staged at loff[b] + its rank) goes to fine_off[f0 + b] + gbase[b] +
-    // rank = base0 + gbase'[b] + i, with gbase'[b] = fine_off[f0 + b] - base0 + gbase[b] - loff[b]:
-    // never negative (loff[b] counts this chunk's part of the buckets before b) and below the
-    // super bucket's 32-bit size, so the write-out needs no global load per element.
+    // Each bucket claims its run of the fine bucket (fine_cur) and gets its offset in the
+    // chunk's staging (loff, exclusive).  Element i of bucket b (staged at loff[b] + its rank)
+    // goes to fine_off[f0 + b] + claim + rank = base0 + gbase'[b] + i, with gbase'[b] =
+    // fine_off[f0 + b] - base0 + claim - loff[b]: never negative (loff[b] counts this chunk's
+    // part of the buckets before b) and below the super bucket's 32-bit size, so the write-out
+    // needs no global load per element.
     const unsigned long long base0 = fine_off[f0];
-    for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) {
-        sm.cur[i] = 0;
-        sm.gbase[i] = (uint32_t)(fine_off[f0 + i] - base0) + sm.gbase[i] - sm.loff[i];
+    const uint32_t per = (F + blockDim.x - 1) / blockDim.x;
+    if (per <= FINE_BOOK) {
+        // a thread's (at most FINE_BOOK) consecutive buckets: their claims are in flight while the
+        // block scans the counts
+        const uint32_t b0 = threadIdx.x * per;
+        uint32_t c[FINE_BOOK], g[FINE_BOOK], sum = 0;
+#pragma unroll
+        for (int q = 0; q < FINE_BOOK; q++) {
+            const uint32_t i = b0 + q;
+            c[q] = ((uint32_t)q < per && i < F) ? sm.cur[i] : 0u;
+            g[q] = c[q] ? atomicAdd(&fine_cur[f0 + i], c[q]) : 0u;
+            sum += c[q];
+        }
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const uint32_t inc = warp_inclusive_scan(sum);
+        if (lane == 31) sm.ws[warp] = inc;
+        __syncthreads();
+        uint32_t ex = inc - sum;
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            if (q < warp) ex += sm.ws[q];
+#pragma unroll
+        for (int q = 0; q < FINE_BOOK; q++) {
+            const uint32_t i = b0 + q;
+            if ((uint32_t)q < per && i < F) {
+                sm.loff[i] = ex;
+                sm.gbase[i] = (uint32_t)(fine_off[f0 + i] - base0) + g[q] - ex;
+                ex += c[q];
+            }
+        }
+    } else {
+        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) {
+            sm.loff[i] = sm.cur[i];
+            sm.gbase[i] = sm.cur[i] ? atomicAdd(&fine_cur[f0 + i], sm.cur[i]) : 0u;
+        }
+        __syncthreads();
+        block_scan_array(sm.loff, F, sm.ws);
+        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x)
+            sm.gbase[i] = (uint32_t)(fine_off[f0 + i] - base0) + sm.gbase[i] - sm.loff[i];
     }
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < FINE_PER_THREAD; q++) {
         if (q * 256 + threadIdx.x >= len) continue;
         const uint32_t bkt = (bk[q >> 1] >> (16 * (q & 1))) & 0xffffu;
-        const uint32_t pos = sm.loff[bkt] + atomicAdd(&sm.cur[bkt], 1u);
+        const uint32_t pos = atomicAdd(&sm.loff[bkt], 1u);  // loff runs through the bucket's staging
         sm.key[pos] = kk[q];
         sm.bits[pos] = (uint16_t)(bb[q >> 1] >> (16 * (q & 1)));
         sm.bkt[pos] = (uint16_t)bkt;
