@@ -2392,36 +2392,29 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
             a.heads[r].slot = (uint32_t)sl;
         }
     }
-    for (uint32_t c0 = 0; c0 < M; c0 += BATCH * blockDim.x) {
-        if (c0) {
-#pragma unroll
-            for (int q = 0; q < BATCH; q++) {
-                const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
-                kk[q] = i < M ? okey[i] : (K)0;
-                bb[q] = i < M ? (uint32_t)obits[i] : 0u;
-            }
-        }
-        // In groups of four: the home slots are read first, all four loads in flight (a key
-        // never leaves the slot it was put in, so a plain read that shows it is final); an
-        // occurrence whose key is not in its home slot takes the probe with compare-and-swap.
-#pragma unroll
-        for (int g = 0; g < BATCH; g += 4) {
+    // In groups of four: the home slots are read first, all four loads in flight (a key never
+    // leaves the slot it was put in, so a plain read that shows it is final); an occurrence
+    // whose key is not in its home slot takes the probe with compare-and-swap.  The thread's
+    // occurrences are i = q * blockDim.x + threadIdx.x; with 64-bit keys two groups are held
+    // in registers, and the loads of the group after next go out as soon as a group is
+    // inserted, so they land while the next one is.
+    if constexpr (BATCH == 8) {
+        auto insert4 = [&](const K *kq, const uint32_t *bq, uint32_t q0) {
             uint32_t hm[4];
             K cur[4];
-#pragma unroll
+    #pragma unroll
             for (int u = 0; u < 4; u++) {
-                hm[u] = agg_home(kk[g + u]);
+                hm[u] = agg_home(kq[u]);
                 cur[u] = sm.key1[hm[u]];
             }
-#pragma unroll
+    #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const int q = g + u;
-                const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
+                const uint32_t i = (q0 + u) * blockDim.x + threadIdx.x;
                 if (i >= M) continue;
                 int sl = (int)hm[u];
-                if (cur[u] != kk[q] + 1) {
+                if (cur[u] != kq[u] + 1) {
                     uint32_t claimed = 0;
-                    sl = AggTable<K>::insert(sm.key1, kk[q], hm[u], claimed);
+                    sl = AggTable<K>::insert(sm.key1, kq[u], hm[u], claimed);
                     if (sl < 0) {
                         sm.fail = 1;
                         continue;
@@ -2429,7 +2422,62 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
                     if (claimed) atomicAdd(&sm.n, 1u);
                 }
                 atomicAdd(&sm.cnt[sl], 1u);  // no result used: both are fire-and-forget reductions
-                if (bb[q]) atomicOr(&sm.meta[sl], bb[q]);
+                if (bq[u]) atomicOr(&sm.meta[sl], bq[u]);
+            }
+        };
+        auto load4 = [&](K *kq, uint32_t *bq, uint32_t q0) {
+    #pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t i = (q0 + u) * blockDim.x + threadIdx.x;
+                kq[u] = i < M ? okey[i] : (K)0;
+                bq[u] = i < M ? (uint32_t)obits[i] : 0u;
+            }
+        };
+        for (uint32_t q0 = 0; q0 * blockDim.x < M; q0 += 8) {
+            insert4(kk, bb, q0);
+            load4(kk, bb, q0 + 8);
+            if ((q0 + 4) * blockDim.x < M) {
+                insert4(kk + 4, bb + 4, q0 + 4);
+                load4(kk + 4, bb + 4, q0 + 12);
+            }
+        }
+    } else {
+        for (uint32_t c0 = 0; c0 < M; c0 += BATCH * blockDim.x) {
+            if (c0) {
+#pragma unroll
+                for (int q = 0; q < BATCH; q++) {
+                    const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
+                    kk[q] = i < M ? okey[i] : (K)0;
+                    bb[q] = i < M ? (uint32_t)obits[i] : 0u;
+                }
+            }
+#pragma unroll
+            for (int g = 0; g < BATCH; g += 4) {
+                uint32_t hm[4];
+                K cur[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    hm[u] = agg_home(kk[g + u]);
+                    cur[u] = sm.key1[hm[u]];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int q = g + u;
+                    const uint32_t i = c0 + q * blockDim.x + threadIdx.x;
+                    if (i >= M) continue;
+                    int sl = (int)hm[u];
+                    if (cur[u] != kk[q] + 1) {
+                        uint32_t claimed = 0;
+                        sl = AggTable<K>::insert(sm.key1, kk[q], hm[u], claimed);
+                        if (sl < 0) {
+                            sm.fail = 1;
+                            continue;
+                        }
+                        if (claimed) atomicAdd(&sm.n, 1u);
+                    }
+                    atomicAdd(&sm.cnt[sl], 1u);
+                    if (bb[q]) atomicOr(&sm.meta[sl], bb[q]);
+                }
             }
         }
     }
