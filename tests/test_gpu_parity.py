@@ -341,3 +341,28 @@ def test_memory_limit_between_counted_and_uncounted_scatter():
     assert base["super_counted"] == 0 and st["super_counted"] == 1  # the counting pass ran
     assert (st["nodes"], st["kmers"], st["read_heads"]) == (ref.nodes, ref.kmers, ref.read_heads)
     assert go.normalize(rec) == go.normalize(ref.records)
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_long_reads_read_heads_from_global_memory(ctx, algo):
+    """600 bp pairs: the read heads' sequences are longer than the head writer stages in shared
+    memory, so every head reads its letters from global memory."""
+    rng = np.random.Generator(np.random.PCG64(91))
+    g = synth.random_genome(rng, 30_000)
+    mates = synth.simulate_chunk(rng, g, 120, 600, True, 1400, 50, 0.01, 0.002)
+    text = synth.readid_lines(0, mates).tobytes()
+    assert_same(ctx, text, 31, algorithm=algo)
+
+
+def test_mixed_read_lengths_in_one_job(ctx):
+    """150 bp single reads and 300 bp pairs in one job (the head writer's slots follow the
+    longest sequence; the 150 bp heads use part of theirs), and a text that starts and ends
+    inside a staged chunk."""
+    rng = np.random.Generator(np.random.PCG64(92))
+    g = synth.random_genome(rng, 20_000)
+    short = synth.simulate_chunk(rng, g, 400, 150, False, None, None, 0.01, 0.0)
+    long_ = synth.simulate_chunk(rng, g, 200, 300, True, 700, 30, 0.01, 0.002)
+    text = synth.readid_lines(0, short).tobytes() + synth.readid_lines(1000, long_).tobytes()
+    assert_same(ctx, text, 25)
+    # no trailing newline, and the last read's letters run to the end of the text
+    assert_same(ctx, text[:-1], 25)
