@@ -2589,6 +2589,7 @@ __global__ void __launch_bounds__(256, sizeof(K) == 8 ? 4 : 3) k_aggregate(AggAr
                 mk = head_sort_key(sm.rank_of_slot[p_slot], p_h.uuid);
             }
             uint32_t rank = 0;
+#pragma unroll 4
             for (int j = 0; j < (int)hc; j++) {
                 const unsigned long long kj = shfl64(mk, j);
                 const uint32_t vj = __shfl_sync(full, mv, j);
@@ -3100,21 +3101,30 @@ __device__ __forceinline__ uint32_t seq_chunks(uintptr_t a, uint32_t L) {
 }
 
 // Warp-collective: each lane's sequence (where `want`) into the lane's slot of `slots` (seqc
-// chunks per lane), one sequence after another, a chunk per lane, by asynchronous copies (the
-// text's first and last chunk, which may reach past it, by plain loads).
+// chunks per lane) by asynchronous copies (the text's first and last chunk, which may reach past
+// it, by plain loads).  The warp's chunks are numbered through a prefix over the lanes' counts
+// and taken 32 at a time, a chunk per lane; a chunk's lane is found by a 5-step search over
+// that prefix.
 __device__ __forceinline__ void stage_seqs(uint4 *slots, uint32_t seqc, bool want, uintptr_t a, uint32_t L,
                                            const uint8_t *text, unsigned long long n_text, int lane) {
     const unsigned full = 0xffffffffu;
     const uintptr_t tb = (uintptr_t)text, te = tb + n_text;
-    uint32_t pend = __ballot_sync(full, want);
-    while (pend) {
-        const int q = __ffs(pend) - 1;
-        pend &= pend - 1;
-        const uintptr_t aq = (uintptr_t)shfl64((unsigned long long)a, q);
-        const uint32_t Lq = __shfl_sync(full, L, q);
-        const uint32_t j = (uint32_t)lane;
-        if (j < seq_chunks(aq, Lq)) {  // at most seqc <= 31: `want` is only set when it fits
-            const uintptr_t c = seq_chunk0(aq) + 16ull * j;
+    const uint32_t cnt = want ? seq_chunks(a, L) : 0u;  // at most seqc <= 31: `want` is only set when it fits
+    const unsigned long long c0 = (unsigned long long)seq_chunk0(a);
+    const uint32_t incl = warp_inclusive_scan(cnt), excl = incl - cnt;
+    const uint32_t total = __shfl_sync(full, incl, 31);
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t idx = base + (uint32_t)lane;
+        // the last lane whose chunks start at or before idx owns it
+        uint32_t q = 0;
+#pragma unroll
+        for (uint32_t s = 16; s; s >>= 1) {
+            const uint32_t e = __shfl_sync(full, excl, (int)(q + s));
+            if (e <= idx) q += s;
+        }
+        const uint32_t j = idx - __shfl_sync(full, excl, (int)q);
+        const uintptr_t c = (uintptr_t)shfl64(c0, (int)q) + 16ull * j;
+        if (idx < total) {
             uint4 *dst = slots + (size_t)q * seqc + j;
             if (c >= tb && c + 16 <= te)
                 cp_async16(dst, reinterpret_cast<const void *>(c));
