@@ -1685,11 +1685,12 @@ void launch_sample_occ(const LineRec *lines, const uint32_t *reads, uint32_t n_r
 }
 
 // ---- A2 -------------------------------------------------------------------------------------
-// A round's k-mers stay in registers between counting and placing them (ten per thread; the
-// 128-bit walk, done twice, cost more than the registers of its cache).
+// A round's k-mers stay in registers between counting and placing them (ten per thread with
+// 64-bit keys, where more spill; twelve with 128-bit keys, whose walk, done twice, cost more
+// than the registers of its cache).
 template <class K> struct SuperRound {
     static constexpr bool CACHE = true;
-    static constexpr int N = 10;  // k-mers per thread per round
+    static constexpr int N = sizeof(K) == 8 ? 10 : 12;  // k-mers per thread per round
 };
 
 // shared layout of k_scatter_super: staging for one round, then four S-entry arrays
